@@ -1,0 +1,142 @@
+/*
+ * nbody_gb300.h -- C ABI of the GB300 FMM step (libnbody_gb300.so).
+ *
+ * This is the drop-in boundary below the reference's Simulation interface
+ * (include/nbody/simulation.h:6-37 of duanebyer/nbody).  The C++ class
+ * nbody::CudaSimulation (include/nbody/cuda_simulation.h) implements that
+ * interface on top of these calls, the way OpenClSimulation
+ * (include/nbody/open_cl_simulation.h:19-203) implements it on top of OpenCL.
+ *
+ * Conventions
+ *   - every call returns an int status (NBODY_OK = 0); no exception crosses it;
+ *     nbody_last_error() gives a one-line message for the last failure;
+ *   - plain pointers and sizes only; host arrays are row-major, positions and
+ *     velocities as n x 3 doubles;
+ *   - one context = one CUDA stream on one device; a context is not
+ *     thread-safe, distinct contexts are independent;
+ *   - particle state stays resident on the device between calls; host copies
+ *     happen only in nbody_set_state / nbody_get_state / nbody_compute_forces.
+ */
+#ifndef NBODY_GB300_H
+#define NBODY_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define NBODY_OK 0
+#define NBODY_ERR_INVALID 1      /* bad argument */
+#define NBODY_ERR_CUDA 2         /* CUDA runtime error */
+#define NBODY_ERR_NOMEM 3        /* device allocation failed */
+#define NBODY_ERR_CAPACITY 4     /* a bounded device structure overflowed */
+#define NBODY_ERR_STATE 5        /* call not valid in the current state */
+#define NBODY_ERR_NO_DEVICE 6    /* no CUDA device */
+
+/* precision forms */
+#define NBODY_PREC_FP32 0        /* state and arithmetic in FP32 */
+#define NBODY_PREC_MIXED 1       /* FP64 state and shifts, FP32 offsets and bulk work, compensated sums */
+#define NBODY_PREC_FP64 2        /* everything in FP64 */
+
+/* integrators */
+#define NBODY_INTEG_LEAPFROG 0   /* kick-drift-kick */
+#define NBODY_INTEG_EULER 1      /* v += F/m dt, x += v_old dt (src/open_cl_simulation.cpp:600-607) */
+
+typedef struct nbody_params {
+    int precision;        /* NBODY_PREC_* */
+    int order;            /* Cartesian expansion order 1..8; 1 = the reference's (monopole, constant local field) */
+    int leaf_capacity;    /* bucket capacity (reference: 8, src/open_cl_simulation.cpp:41-47); 1..64 */
+    int max_level;        /* depth cap, <= 21 */
+    double theta;         /* opening angle of the MAC 3/4 (wA+wB)^2/d^2 < theta^2 (src/interaction.cl:3-5,64-79) */
+    double eps;           /* Plummer softening (PARTICLE_RADIUS, src/field.cl:3-5) */
+    double G;             /* coupling (-FORCE_CONSTANT, src/field.cl:7-9) */
+    double dt;            /* time step */
+    int integrator;       /* NBODY_INTEG_* */
+    int fixed_box;        /* 1: root box [box_min, box_min + box_size)^3 as the reference's bounds; 0: data cube per step */
+    double box_min[3];
+    double box_size;
+    int device;           /* CUDA device ordinal */
+} nbody_params;
+
+typedef struct nbody_ctx nbody_ctx;
+
+/* Fills the reference's defaults: FP32, order 1, capacity 8, theta 0.5,
+   eps 0.01, G 1, dt 1e-3, explicit Euler, box [0,1)^3
+   (src/main.cpp:23-27,69, src/interaction.cl:3-5, src/field.cl:3-9). */
+void nbody_default_params(nbody_params* p);
+
+/* Creates a context (replaces OpenClSimulation::initialize,
+   src/open_cl_simulation.cpp:618-681: device selection and setup). */
+int nbody_create(const nbody_params* p, nbody_ctx** out);
+
+/* Releases every device resource of the context. */
+int nbody_destroy(nbody_ctx* c);
+
+/* Uploads particles; arrays are n x 3 (pos, vel) and n (mass, charge);
+   charge may be NULL (charge = mass).  Replaces the particle packing and
+   octree construction of the OpenClSimulation constructor
+   (src/open_cl_simulation.cpp:15-51). Resets the time to 0. */
+int nbody_set_state(nbody_ctx* c, int64_t n, const double* pos, const double* vel, const double* mass,
+                    const double* charge);
+
+/* Downloads the state.  order = 0: current Morton (leaf) order, the order
+   the reference's particles() returns (src/open_cl_simulation.cpp:53-68);
+   order = 1: input order.  Any pointer may be NULL.  ids receives, per row,
+   the input index of that particle. */
+int nbody_get_state(nbody_ctx* c, int order, double* pos, double* vel, double* mass, double* charge, int64_t* ids);
+
+/* Advances nsteps steps of dt (replaces OpenClSimulation::step,
+   src/open_cl_simulation.cpp:70-106); *t_out (may be NULL) receives the
+   time after the last step. */
+int nbody_step(nbody_ctx* c, int nsteps, double* t_out);
+
+/* Accelerations (n x 3) and, if pot != NULL, potential per unit charge (n) at
+   the current positions, in input order, without advancing.  This is the
+   force evaluation that the reference keeps private
+   (computeForceBuffers, src/open_cl_simulation.cpp:486-570). */
+int nbody_compute_forces(nbody_ctx* c, double* acc, double* pot);
+
+/* FP64 diagnostics of the current state: out[0] kinetic energy, out[1]
+   potential energy, out[2..4] momentum, out[5..7] angular momentum,
+   out[8] total mass.  (The reference computes none.) */
+int nbody_diagnostics(nbody_ctx* c, double* out);
+
+/* Number of particles, nodes, leaves and the depth of the last tree. */
+int nbody_tree_info(nbody_ctx* c, int64_t* n, int64_t* nnodes, int64_t* nleaves, int* depth);
+
+/* Copies the last tree for inspection: keys (n, sorted Morton keys), perm
+   (n, input index of each sorted row), nodes (nnodes x 9 int32 rows:
+   level, ix, iy, iz, begin, count, parent, child_begin, nchild; breadth-first).
+   Any pointer may be NULL. */
+int nbody_get_tree(nbody_ctx* c, uint64_t* keys, int64_t* perm, int32_t* nodes);
+
+/* Sizes and contents of the last interaction lists, as (target, source)
+   node pairs.  which = 0: far field (M2L), 1: near field (P2P).  Pass
+   pairs = NULL to get the size only.  Replaces the interaction buffers of
+   computeInteractionBuffers (src/open_cl_simulation.cpp:176-369). */
+int nbody_get_interactions(nbody_ctx* c, int which, int64_t* npairs, int32_t* pairs);
+
+/* Per-phase device times (ms) of the last step: 0 kick/drift + keys, 1 sort +
+   gather, 2 tree, 3 upward pass, 4 traversal + M2L + L2L, 5 near field + L2P
+   + integration.  Timing is enabled by nbody_set_timing(c, 1). */
+int nbody_set_timing(nbody_ctx* c, int on);
+int nbody_phase_times(nbody_ctx* c, float* ms, int n);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+   own work after the step. */
+void* nbody_stream(nbody_ctx* c);
+
+/* Simulated time. */
+int nbody_get_time(nbody_ctx* c, double* t);
+
+/* Message of the last failure on this context (or of the last failed
+   nbody_create when c is NULL). */
+const char* nbody_last_error(nbody_ctx* c);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,793 @@
+// FMM kernels of the step, templated on the precision form and the order.
+//
+// Replaces the reference kernels of src/moment.cl (P2M/M2M),
+// src/interaction.cl (interaction finding), src/field.cl (pair and node
+// fields) and src/force.cl (field -> force), plus the host integration loop
+// of src/open_cl_simulation.cpp:572-616, with:
+//   k_p2m       multipoles of every leaf about its geometric centre, and each
+//               particle's offset from its leaf centre (packed with its charge);
+//   k_m2m       one tree level per launch, children shifted to the parent
+//               centre (translation offsets exact, in the shift precision);
+//   k_traverse  one tree level per launch: a warp per target cell refines its
+//               parent's pending partners (src/interaction.cl:10-100 MAC and
+//               split rules), evaluates every accepted far-field partner at
+//               once (M2L into per-lane accumulators, no interaction buffer),
+//               writes the near-field and still-pending partners as one
+//               contiguous per-target list, and adds the parent's shifted
+//               local expansion (L2L).  Leaf targets descend remaining
+//               partners with a per-warp stack;
+//   k_p2p       a warp per leaf: near-field sums over its partner leaves with
+//               source tiles staged in shared memory, the local expansion
+//               evaluated at each particle (L2P), and the integrator update as
+//               the epilogue.
+// Every per-target sum runs in a fixed order, so results are bitwise
+// reproducible run to run.
+#pragma once
+
+#include "nbody_internal.cuh"
+#include "fmm_ops.inc"
+
+namespace nbfmm {
+
+struct __align__(32) D4 {
+    double x, y, z, w;
+};
+
+template <int MODE> struct Prec;
+template <> struct Prec<NBODY_PREC_FP32> {
+    typedef float R;   // state
+    typedef float S;   // bulk arithmetic (P2P, M2L, P2M, L2P)
+    typedef float H;   // expansions and shifts (M2M, L2L)
+    typedef float4 S4;
+    static constexpr bool kahan = false;
+    static constexpr int trav_warps = 8;
+    static constexpr bool lane_smem = false;
+};
+template <> struct Prec<NBODY_PREC_MIXED> {
+    typedef double R;
+    typedef float S;
+    typedef double H;
+    typedef float4 S4;
+    static constexpr bool kahan = true;
+    static constexpr int trav_warps = 8;
+    static constexpr bool lane_smem = false;
+};
+template <> struct Prec<NBODY_PREC_FP64> {
+    typedef double R;
+    typedef double S;
+    typedef double H;
+    typedef D4 S4;
+    static constexpr bool kahan = false;
+    static constexpr int trav_warps = 1;
+    static constexpr bool lane_smem = true;   // per-lane D and L live in shared memory
+};
+
+constexpr int STK = 512;         // descent stack entries per warp
+constexpr int CAND = 256;        // expanded candidates per chunk (32 partners x 8 children)
+constexpr uint32_t NONE = 0xffffffffu;
+
+__device__ __forceinline__ int mac_accept(long long tcx, long long tcy, long long tcz, long long tw,
+                                          const NodeRec& s, double theta2x4) {
+    long long sx, sy, sz;
+    nb_centre_fine(s, sx, sy, sz);
+    long long dx = sx - tcx, dy = sy - tcy, dz = sz - tcz;
+    long long d2 = dx * dx + dy * dy + dz * dz;
+    long long e = tw + nb_width_fine(s);
+    return 3.0 * (double)e * (double)e < theta2x4 * (double)d2;
+}
+
+// exact centre displacement (a - b) in box units
+__device__ __forceinline__ void disp(const NodeRec& a, const NodeRec& b, double unit, double& dx, double& dy,
+                                     double& dz) {
+    long long ax, ay, az, bx, by, bz;
+    nb_centre_fine(a, ax, ay, az);
+    nb_centre_fine(b, bx, by, bz);
+    dx = (double)(ax - bx) * unit;
+    dy = (double)(ay - by) * unit;
+    dz = (double)(az - bz) * unit;
+}
+
+__device__ __forceinline__ double centre_coord(uint32_t i, int level, double origin, double side) {
+    return origin + ((double)i + 0.5) * (side / (double)(1u << level));
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_xor_t(T v, int o) {
+    return __shfl_xor_sync(0xffffffffu, v, o);
+}
+
+// ---------------------------------------------------------------------------
+// P2M at leaves + particle offsets
+// ---------------------------------------------------------------------------
+template <int MODE, int P>
+__global__ void __launch_bounds__(128) k_p2m(int64_t nleaves, const uint32_t* __restrict__ leaves,
+                                             const NodeRec* __restrict__ nodes, const BoxDev* __restrict__ boxp,
+                                             const typename Prec<MODE>::R* __restrict__ x,
+                                             const typename Prec<MODE>::R* __restrict__ y,
+                                             const typename Prec<MODE>::R* __restrict__ z,
+                                             const typename Prec<MODE>::R* __restrict__ q,
+                                             typename Prec<MODE>::S4* __restrict__ src,
+                                             typename Prec<MODE>::H* __restrict__ M, float* __restrict__ M32) {
+    typedef typename Prec<MODE>::R R;
+    typedef typename Prec<MODE>::S S;
+    typedef typename Prec<MODE>::H H;
+    constexpr int T = nb_terms<P>::value;
+    __shared__ S pw[4][32][3][P + 1];
+    __shared__ S qq[4][32];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int64_t w = (int64_t)blockIdx.x * 4 + wib;
+    if (w >= nleaves) return;
+    const uint32_t k = leaves[w];
+    const NodeRec nd = nodes[k];
+    const BoxDev b = *boxp;
+    const R cx = (R)centre_coord(nd.ix, nd.level, b.ox, b.side);
+    const R cy = (R)centre_coord(nd.iy, nd.level, b.oy, b.side);
+    const R cz = (R)centre_coord(nd.iz, nd.level, b.oz, b.side);
+    constexpr int NPL = (T + 31) / 32;   // coefficients per lane
+    int ex[NPL][3];
+    S acc[NPL];
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        acc[j] = S(0);
+        int a = lane + 32 * j;
+        int aa = a < T ? a : 0;
+        ex[j][0] = nb_mi[aa][0]; ex[j][1] = nb_mi[aa][1]; ex[j][2] = nb_mi[aa][2];
+    }
+    const uint32_t end = nd.begin + nd.count;
+    for (uint32_t base = nd.begin; base < end; base += 32) {
+        uint32_t i = base + lane;
+        if (i < end) {
+            S yx = (S)(x[i] - cx), yy = (S)(y[i] - cy), yz = (S)(z[i] - cz), qi = (S)q[i];
+            typename Prec<MODE>::S4 o;
+            o.x = yx; o.y = yy; o.z = yz; o.w = qi;
+            src[i] = o;
+            S v[3] = {yx, yy, yz};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                S p = S(1);
+#pragma unroll
+                for (int e = 0; e <= P; ++e) { pw[wib][lane][d][e] = p; p *= v[d]; }
+            }
+            qq[wib][lane] = qi;
+        }
+        __syncwarp();
+        int cnt = end - base < 32 ? (int)(end - base) : 32;
+        for (int jj = 0; jj < cnt; ++jj) {
+            S qj = qq[wib][jj];
+#pragma unroll
+            for (int j = 0; j < NPL; ++j)
+                acc[j] = nb_fma(qj, pw[wib][jj][0][ex[j][0]] * pw[wib][jj][1][ex[j][1]] * pw[wib][jj][2][ex[j][2]],
+                                acc[j]);
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        int a = lane + 32 * j;
+        if (a < T) {
+            H v = (H)acc[j] * (H)nb_invfact[a];
+            M[(int64_t)k * T + a] = v;
+            if (M32) M32[(int64_t)k * T + a] = (float)v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// M2M: one level, warp per internal node
+// ---------------------------------------------------------------------------
+template <int MODE, int P>
+__global__ void __launch_bounds__(128) k_m2m(int lo, int hi, const NodeRec* __restrict__ nodes,
+                                             const BoxDev* __restrict__ boxp, typename Prec<MODE>::H* __restrict__ M,
+                                             float* __restrict__ M32) {
+    typedef typename Prec<MODE>::H H;
+    constexpr int T = nb_terms<P>::value;
+    __shared__ H sM[4][T];
+    __shared__ H sY[4][T];
+    __shared__ H spw[4][3][P + 1];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int k = lo + blockIdx.x * 4 + wib;
+    if (k >= hi) return;
+    const NodeRec nd = nodes[k];
+    if (nd.nchild == 0) return;
+    const double unit = boxp->unit;
+    const unsigned short* st = Tabs<P>::m2m_start();
+    const unsigned short* pr = Tabs<P>::m2m_pairs();
+    constexpr int NPL = (T + 31) / 32;
+    H acc[NPL];
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) acc[j] = H(0);
+    for (int c = 0; c < nd.nchild; ++c) {
+        const int ch = nd.child_begin + c;
+        const NodeRec cn = nodes[ch];
+        double dx, dy, dz;
+        disp(cn, nd, unit, dx, dy, dz);
+        for (int a = lane; a < T; a += 32) sM[wib][a] = M[(int64_t)ch * T + a];
+        if (lane < 3) {
+            H d = (H)(lane == 0 ? dx : lane == 1 ? dy : dz), p = H(1);
+            for (int e = 0; e <= P; ++e) { spw[wib][lane][e] = p; p *= d; }
+        }
+        __syncwarp();
+        for (int a = lane; a < T; a += 32)
+            sY[wib][a] = spw[wib][0][nb_mi[a][0]] * spw[wib][1][nb_mi[a][1]] * spw[wib][2][nb_mi[a][2]] *
+                         (H)nb_invfact[a];
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < NPL; ++j) {
+            int a = lane + 32 * j;
+            if (a < T) {
+                H s = acc[j];
+                for (int u = st[a]; u < st[a + 1]; ++u) s = nb_fma(sM[wib][pr[2 * u]], sY[wib][pr[2 * u + 1]], s);
+                acc[j] = s;
+            }
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        int a = lane + 32 * j;
+        if (a < T) {
+            M[(int64_t)k * T + a] = acc[j];
+            if (M32) M32[(int64_t)k * T + a] = (float)acc[j];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// traversal round 0: the root
+// ---------------------------------------------------------------------------
+template <int MODE, int P>
+__global__ void k_root(const NodeRec* __restrict__ nodes, typename Prec<MODE>::H* __restrict__ L,
+                       uint32_t* pend_off, uint32_t* pend_cnt, uint32_t* pend_list, uint32_t* p2p_off,
+                       uint32_t* p2p_cnt, uint32_t* p2p_list, int32_t* info) {
+    constexpr int T = nb_terms<P>::value;
+    for (int a = threadIdx.x; a < T; a += blockDim.x) L[a] = 0;
+    if (threadIdx.x == 0) {
+        const bool leaf = nodes[0].nchild == 0;
+        uint32_t* tail = (uint32_t*)&info[leaf ? INFO_P2P_TAIL : INFO_PEND_TAIL];
+        uint32_t o = *tail;
+        *tail = o + 1;
+        if (leaf) { p2p_list[o] = 0; p2p_off[0] = o; p2p_cnt[0] = 1; pend_cnt[0] = 0; }
+        else { pend_list[o] = 0; pend_off[0] = o; pend_cnt[0] = 1; p2p_cnt[0] = 0; }
+    }
+}
+
+struct TravArgs {
+    const NodeRec* nodes;
+    const BoxDev* box;
+    const void* Mm2l;       // S*: multipoles read by M2L
+    void* L;                // H*
+    uint32_t *pend_off, *pend_cnt, *pend_list, *p2p_off, *p2p_cnt, *p2p_list;
+    uint32_t pend_cap, p2p_cap;
+    uint32_t *m2l_off, *m2l_cnt, *m2l_list;   // null unless the far-field lists are recorded
+    uint32_t m2l_cap;
+    int32_t* info;
+    double theta2x4;        // 4 theta^2
+    double eps2;
+    int lo, hi;             // target node range (one level)
+};
+
+template <int MODE, int P>
+struct TravSmem {
+    typedef typename Prec<MODE>::H H;
+    static constexpr int T = nb_terms<P>::value;
+    static constexpr size_t lane_arrays =
+        Prec<MODE>::lane_smem ? (size_t)2 * 32 * T * sizeof(typename Prec<MODE>::S) : 0;
+    static constexpr size_t per_warp_raw =
+        sizeof(uint32_t) * (CAND + STK + 64) + sizeof(H) * (3 * T + 3 * (P + 1)) + lane_arrays;
+    static constexpr size_t per_warp = (per_warp_raw + 255) / 256 * 256;
+};
+
+template <int MODE, int P>
+__global__ void __launch_bounds__(32 * Prec<MODE>::trav_warps, 1) k_traverse(TravArgs A) {
+    typedef typename Prec<MODE>::S S;
+    typedef typename Prec<MODE>::H H;
+    constexpr int T = nb_terms<P>::value;
+    constexpr bool LS = Prec<MODE>::lane_smem;
+    extern __shared__ __align__(256) unsigned char smem_raw[];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int t = A.lo + blockIdx.x * Prec<MODE>::trav_warps + wib;
+    if (t >= A.hi) return;
+    unsigned char* ws = smem_raw + (size_t)wib * TravSmem<MODE, P>::per_warp;
+    uint32_t* cand = (uint32_t*)ws;
+    uint32_t* stk = cand + CAND;
+    uint32_t* batch = stk + STK;
+    H* sLp = (H*)(batch + 64);
+    H* sY = sLp + T;
+    H* sLs = sY + T;
+    H* spw = sLs + T;
+    S* laneD = (S*)(spw + 3 * (P + 1));
+    S* laneL = laneD + 32 * T;
+
+    const NodeRec nt = A.nodes[t];
+    const bool tleaf = nt.nchild == 0;
+    long long tcx, tcy, tcz;
+    nb_centre_fine(nt, tcx, tcy, tcz);
+    const long long tw = nb_width_fine(nt);
+    const double unit = A.box->unit;
+    const int par = nt.parent;
+    const uint32_t pb = A.pend_off[par], pc = A.pend_cnt[par];
+    const S* Msrc = (const S*)A.Mm2l;
+
+    // per-lane partial local expansion: registers (FP32 forms) or a shared-memory column (FP64)
+    S Lreg[LS ? 1 : T];
+    if constexpr (LS) {
+        for (int a = 0; a < T; ++a) laneL[a * 32 + lane] = S(0);
+    } else {
+#pragma unroll
+        for (int a = 0; a < T; ++a) Lreg[a] = S(0);
+    }
+
+    uint32_t out_base = 0, n_out = 0, m_base = 0, m_pos = 0;
+    bool can_write = false, m_write = false;
+    int bn = 0;
+    uint32_t* out_list = tleaf ? A.p2p_list : A.pend_list;
+
+    auto m2l_batch = [&](int cnt) {
+        if (lane < cnt) {
+            const uint32_t s = batch[lane];
+            const NodeRec sn = A.nodes[s];
+            long long sx, sy, sz;
+            nb_centre_fine(sn, sx, sy, sz);
+            const S dx = (S)((double)(tcx - sx) * unit), dy = (S)((double)(tcy - sy) * unit),
+                    dz = (S)((double)(tcz - sz) * unit);
+            if constexpr (LS) {
+                Ops<S, P>::template derivs<32>(dx, dy, dz, (S)A.eps2, laneD + lane);
+                Ops<S, P>::template m2l<32>(Msrc + (int64_t)s * T, laneD + lane, laneL + lane);
+            } else {
+                S D[T];
+                Ops<S, P>::template derivs<1>(dx, dy, dz, (S)A.eps2, D);
+                Ops<S, P>::template m2l<1>(Msrc + (int64_t)s * T, D, Lreg);
+            }
+        }
+    };
+
+    for (int pass = 0; pass < 2; ++pass) {
+        uint32_t wpos = 0;
+        int top = 0;
+        m_pos = 0;
+        auto classify = [&](uint32_t s) {
+            const bool valid = s != NONE;
+            NodeRec sn;
+            if (valid) sn = A.nodes[s];
+            const bool approx = valid && (int)s != t && mac_accept(tcx, tcy, tcz, tw, sn, A.theta2x4);
+            const bool sleaf = valid && sn.nchild == 0;
+            const bool out = valid && !approx && (!tleaf || sleaf);
+            const bool desc = valid && !approx && tleaf && !sleaf;
+            const uint32_t mo = __ballot_sync(0xffffffffu, out);
+            if (out && pass == 1 && can_write) {
+                uint32_t pos = wpos + __popc(mo & lanemask_lt());
+                if (pos < n_out) out_list[out_base + pos] = s;
+            }
+            wpos += __popc(mo);
+            const uint32_t md = __ballot_sync(0xffffffffu, desc);
+            if (desc) {
+                int pos = top + __popc(md & lanemask_lt());
+                if (pos < STK) stk[pos] = s;
+                else atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_STACK);
+            }
+            top = min(top + __popc(md), STK);
+            const uint32_t ma = __ballot_sync(0xffffffffu, approx);
+            if (A.m2l_list) {
+                if (pass == 1 && approx && m_write) A.m2l_list[m_base + m_pos + __popc(ma & lanemask_lt())] = s;
+                m_pos += __popc(ma);
+            }
+            if (pass == 1) {
+                if (approx) batch[bn + __popc(ma & lanemask_lt())] = s;
+                bn += __popc(ma);
+                __syncwarp();
+                if (bn >= 32) {
+                    m2l_batch(32);
+                    __syncwarp();
+                    if (lane < bn - 32) batch[lane] = batch[32 + lane];
+                    bn -= 32;
+                    __syncwarp();
+                }
+            }
+        };
+        auto drain_stack = [&]() {
+            while (top > 0) {
+                const int kk = min(top, 4);
+                const int qn = lane >> 3, ci = lane & 7;
+                uint32_t s2 = NONE;
+                if (qn < kk) {
+                    const NodeRec pn = A.nodes[stk[top - 1 - qn]];
+                    if (ci < pn.nchild) s2 = (uint32_t)(pn.child_begin + ci);
+                }
+                __syncwarp();
+                top -= kk;
+                classify(s2);
+                __syncwarp();
+            }
+        };
+        for (uint32_t chunk = 0; chunk < pc; chunk += 32) {
+            const uint32_t j = chunk + lane;
+            uint32_t s = NONE, ns = 0;
+            NodeRec sn;
+            sn.nchild = 0;
+            sn.child_begin = 0;
+            if (j < pc) {
+                s = A.pend_list[pb + j];
+                sn = A.nodes[s];
+                ns = sn.nchild ? sn.nchild : 1u;
+            }
+            const uint32_t inc = warp_incl_scan(ns);
+            const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+            const uint32_t ex = inc - ns;
+            if (ns == 1 && sn.nchild == 0) cand[ex] = s;
+            else
+                for (uint32_t u = 0; u < ns; ++u) cand[ex + u] = (uint32_t)(sn.child_begin + u);
+            __syncwarp();
+            for (uint32_t g = 0; g < total; g += 32) {
+                const uint32_t s2 = g + lane < total ? cand[g + lane] : NONE;
+                classify(s2);
+            }
+            __syncwarp();
+            drain_stack();
+        }
+        if (pass == 0) {
+            n_out = wpos;
+            uint32_t base = 0;
+            int ok = 0;
+            if (lane == 0) {
+                uint32_t* tail = (uint32_t*)&A.info[tleaf ? INFO_P2P_TAIL : INFO_PEND_TAIL];
+                const uint32_t cap = tleaf ? A.p2p_cap : A.pend_cap;
+                base = atomicAdd(tail, n_out);
+                ok = (uint64_t)base + n_out <= cap;
+                if (!ok) atomicOr((unsigned int*)&A.info[INFO_ERR], tleaf ? NB_ERRBIT_P2P_CAP : NB_ERRBIT_PEND_CAP);
+            }
+            out_base = __shfl_sync(0xffffffffu, base, 0);
+            can_write = __shfl_sync(0xffffffffu, ok, 0);
+            if (A.m2l_list) {
+                uint32_t mb = 0;
+                int mok = 0;
+                if (lane == 0) {
+                    mb = atomicAdd((uint32_t*)&A.info[INFO_M2L_TAIL], m_pos);
+                    mok = (uint64_t)mb + m_pos <= A.m2l_cap;
+                    if (!mok) atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_M2L_CAP);
+                    A.m2l_off[t] = mb;
+                    A.m2l_cnt[t] = mok ? m_pos : 0;
+                }
+                m_base = __shfl_sync(0xffffffffu, mb, 0);
+                m_write = __shfl_sync(0xffffffffu, mok, 0);
+            }
+            if (lane == 0) {
+                if (tleaf) {
+                    A.p2p_off[t] = out_base; A.p2p_cnt[t] = can_write ? n_out : 0;
+                    A.pend_cnt[t] = 0;
+                } else {
+                    A.pend_off[t] = out_base; A.pend_cnt[t] = can_write ? n_out : 0;
+                    A.p2p_cnt[t] = 0;
+                }
+            }
+        }
+    }
+    __syncwarp();
+    if (bn > 0) m2l_batch(bn);
+    __syncwarp();
+
+    // reduce the per-lane partial local expansions (fixed butterfly order)
+#pragma unroll
+    for (int a = 0; a < T; ++a) {
+        S v;
+        if constexpr (LS) v = laneL[a * 32 + lane];
+        else v = Lreg[a];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += shfl_xor_t(v, o);
+        if ((a & 31) == lane) sLs[a] = (H)v;
+    }
+    // L2L from the parent + store
+    const NodeRec pn = A.nodes[par];
+    double dx, dy, dz;
+    disp(nt, pn, unit, dx, dy, dz);
+    H* Lg = (H*)A.L;
+    for (int a = lane; a < T; a += 32) sLp[a] = Lg[(int64_t)par * T + a];
+    if (lane < 3) {
+        H d = (H)(lane == 0 ? dx : lane == 1 ? dy : dz), p = H(1);
+        for (int e = 0; e <= P; ++e) { spw[lane * (P + 1) + e] = p; p *= d; }
+    }
+    __syncwarp();
+    for (int a = lane; a < T; a += 32)
+        sY[a] = spw[nb_mi[a][0]] * spw[(P + 1) + nb_mi[a][1]] * spw[2 * (P + 1) + nb_mi[a][2]] * (H)nb_invfact[a];
+    __syncwarp();
+    const unsigned short* st = Tabs<P>::l2l_start();
+    const unsigned short* pr = Tabs<P>::l2l_pairs();
+    for (int a = lane; a < T; a += 32) {
+        H s = sLs[a];
+        for (int u = st[a]; u < st[a + 1]; ++u) s = nb_fma(sLp[pr[2 * u]], sY[pr[2 * u + 1]], s);
+        Lg[(int64_t)t * T + a] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// near field + L2P + integrator epilogue: warp per leaf
+// ---------------------------------------------------------------------------
+struct P2PArgs {
+    const uint32_t* leaves;
+    int64_t nleaves;
+    const NodeRec* nodes;
+    const BoxDev* box;
+    const void* src;        // S4*
+    const void* L;          // H*
+    const uint32_t *p2p_off, *p2p_cnt, *p2p_list;
+    void *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az;   // R*
+    const void *m, *q;      // R*
+    void* pot;              // R* or null
+    double eps2, G, dt;
+    int integ;
+};
+
+template <typename S>
+__device__ __forceinline__ void kahan_add(S& sum, S& comp, S v) {
+    S yv = v - comp;
+    S tv = sum + yv;
+    comp = (tv - sum) - yv;
+    sum = tv;
+}
+
+constexpr int P2P_WARPS = 4;
+constexpr int P2P_TILE = 32;
+
+template <int MODE, int P, bool POT>
+__global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p(P2PArgs A) {
+    typedef typename Prec<MODE>::R R;
+    typedef typename Prec<MODE>::S S;
+    typedef typename Prec<MODE>::H H;
+    typedef typename Prec<MODE>::S4 S4;
+    constexpr int T = nb_terms<P>::value;
+    constexpr bool KH = Prec<MODE>::kahan;
+    __shared__ S4 tile[P2P_WARPS][4][P2P_TILE];
+    __shared__ S sL[P2P_WARPS][T];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int64_t w = (int64_t)blockIdx.x * P2P_WARPS + wib;
+    if (w >= A.nleaves) return;
+    const uint32_t k = A.leaves[w];
+    const NodeRec nt = A.nodes[k];
+    const double unit = A.box->unit;
+    const S4* src = (const S4*)A.src;
+    const H* Lg = (const H*)A.L;
+    for (int a = lane; a < T; a += 32) sL[wib][a] = (S)Lg[(int64_t)k * T + a];
+    const uint32_t cnt_t = nt.count;
+    const int CT = cnt_t <= 4 ? 4 : cnt_t <= 8 ? 8 : cnt_t <= 16 ? 16 : 32;
+    const int NG = 32 / CT, grp = lane / CT, gl = lane % CT;
+    const uint32_t loff = A.p2p_off[k], lcnt = A.p2p_cnt[k];
+    const S eps2 = (S)A.eps2;
+    __syncwarp();
+    for (uint32_t tc = 0; tc < cnt_t; tc += CT) {
+        const uint32_t ti = tc + gl;
+        const bool tvalid = ti < cnt_t;
+        const uint32_t i = nt.begin + (tvalid ? ti : 0);
+        const S4 yi = src[i];
+        S ex = 0, ey = 0, ez = 0, ps = 0, cx = 0, cy = 0, cz = 0, cp = 0;
+        const uint32_t rounds = (lcnt + NG - 1) / NG;
+        for (uint32_t rr = 0; rr < rounds; ++rr) {
+            const uint32_t li = rr * NG + grp;
+            const bool has = li < lcnt;
+            uint32_t s = 0, scount = 0, sbeg = 0;
+            S dx = 0, dy = 0, dz = 0;
+            if (has) {
+                s = A.p2p_list[loff + li];
+                const NodeRec sn = A.nodes[s];
+                scount = sn.count;
+                sbeg = sn.begin;
+                double ddx, ddy, ddz;
+                disp(sn, nt, unit, ddx, ddy, ddz);
+                dx = (S)ddx; dy = (S)ddy; dz = (S)ddz;
+            }
+            uint32_t mx = scount;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            for (uint32_t sb = 0; sb < mx; sb += P2P_TILE) {
+                for (int e = gl; e < P2P_TILE; e += CT) {
+                    const uint32_t j = sb + e;
+                    S4 v;
+                    if (j < scount) {
+                        v = src[sbeg + j];
+                        v.x += dx; v.y += dy; v.z += dz;
+                    } else {
+                        v.x = 0; v.y = 0; v.z = 0; v.w = 0;
+                    }
+                    tile[wib][grp][e] = v;
+                }
+                __syncwarp();
+                const int nj = scount > sb ? min((int)(scount - sb), P2P_TILE) : 0;
+                S px = 0, py = 0, pz = 0, pp = 0;
+#pragma unroll 4
+                for (int e = 0; e < nj; ++e) {
+                    const S4 sj = tile[wib][grp][e];
+                    const S rx = sj.x - yi.x, ry = sj.y - yi.y, rz = sj.z - yi.z;
+                    const S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
+                    S inv = s2 > S(0) ? nb_rsqrt(s2) : S(0);
+                    if (POT && s == k && sb + e == ti) inv = S(0);
+                    const S w3 = sj.w * inv * inv * inv;
+                    px = nb_fma(rx, w3, px);
+                    py = nb_fma(ry, w3, py);
+                    pz = nb_fma(rz, w3, pz);
+                    if (POT) pp = nb_fma(sj.w, inv, pp);
+                }
+                if (KH) {
+                    kahan_add(ex, cx, px); kahan_add(ey, cy, py); kahan_add(ez, cz, pz);
+                    if (POT) kahan_add(ps, cp, pp);
+                } else {
+                    ex += px; ey += py; ez += pz;
+                    if (POT) ps += pp;
+                }
+                __syncwarp();
+            }
+        }
+        // combine the source groups in a fixed order, in the state precision
+        R Ex = (R)ex - (R)cx, Ey = (R)ey - (R)cy, Ez = (R)ez - (R)cz, Ps = (R)ps - (R)cp;
+        for (int o = CT; o < 32; o <<= 1) {
+            Ex += shfl_xor_t(Ex, o); Ey += shfl_xor_t(Ey, o); Ez += shfl_xor_t(Ez, o);
+            if (POT) Ps += shfl_xor_t(Ps, o);
+        }
+        if (grp == 0 && tvalid) {
+            S fx, fy, fz, fp;
+            Ops<S, P>::l2p(sL[wib], yi.x, yi.y, yi.z, fx, fy, fz, fp);
+            Ex += (R)fx; Ey += (R)fy; Ez += (R)fz;
+            if (POT) Ps += (R)fp;
+            const R* mq = (const R*)A.m;
+            const R* qq = (const R*)A.q;
+            const R f = (R)A.G * qq[i] / mq[i];
+            const R axv = f * Ex, ayv = f * Ey, azv = f * Ez;
+            R* X = (R*)A.x; R* Y = (R*)A.y; R* Z = (R*)A.z;
+            R* VX = (R*)A.vx; R* VY = (R*)A.vy; R* VZ = (R*)A.vz;
+            R* AX = (R*)A.ax; R* AY = (R*)A.ay; R* AZ = (R*)A.az;
+            AX[i] = axv; AY[i] = ayv; AZ[i] = azv;
+            if (A.integ == NB_INTEG_KDK_CLOSE) {
+                const R h = (R)(0.5 * A.dt);
+                VX[i] += h * axv; VY[i] += h * ayv; VZ[i] += h * azv;
+            } else if (A.integ == NB_INTEG_EULER) {
+                const R dt = (R)A.dt;
+                const R vx0 = VX[i], vy0 = VY[i], vz0 = VZ[i];
+                VX[i] = vx0 + axv * dt; VY[i] = vy0 + ayv * dt; VZ[i] = vz0 + azv * dt;
+                X[i] += vx0 * dt; Y[i] += vy0 * dt; Z[i] += vz0 * dt;
+            }
+            if (POT) ((R*)A.pot)[i] = -(R)A.G * Ps;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host driver for one (mode, order)
+// ---------------------------------------------------------------------------
+template <int MODE, int P>
+int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
+    typedef typename Prec<MODE>::R R;
+    typedef typename Prec<MODE>::S S;
+    typedef typename Prec<MODE>::H H;
+    typedef typename Prec<MODE>::S4 S4;
+    constexpr int T = nb_terms<P>::value;
+    const int64_t nn = c->nnodes, n = c->n;
+    const int cur = c->cur;
+    NB_TRY(nb_grow(c, c->M, sizeof(H) * T * nn));
+    if (MODE == NBODY_PREC_MIXED) NB_TRY(nb_grow(c, c->M32, sizeof(float) * T * nn));
+    NB_TRY(nb_grow(c, c->L, sizeof(H) * T * nn));
+    NB_TRY(nb_grow(c, c->src, sizeof(S4) * n));
+    NB_TRY(nb_grow(c, c->pend_off, sizeof(uint32_t) * nn));
+    NB_TRY(nb_grow(c, c->pend_cnt, sizeof(uint32_t) * nn));
+    NB_TRY(nb_grow(c, c->p2p_off, sizeof(uint32_t) * nn));
+    NB_TRY(nb_grow(c, c->p2p_cnt, sizeof(uint32_t) * nn));
+    float* M32 = MODE == NBODY_PREC_MIXED ? DP<float>(c->M32) : nullptr;
+    const BoxDev* box = DP<BoxDev>(c->box);
+
+    if (c->timing) cudaEventRecord(c->ev[3], c->st);
+    k_p2m<MODE, P><<<(unsigned)((c->nleaves + 3) / 4), 128, 0, c->st>>>(
+        c->nleaves, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes), box, DP<R>(c->x[cur]), DP<R>(c->y[cur]),
+        DP<R>(c->z[cur]), DP<R>(c->q[cur]), DP<S4>(c->src), DP<H>(c->M), M32);
+    NB_LAUNCHED(c, "p2m");
+    for (int l = c->depth - 1; l >= 0; --l) {
+        const int lo = c->level_start[l], hi = c->level_start[l + 1];
+        if (hi <= lo) continue;
+        k_m2m<MODE, P><<<(unsigned)((hi - lo + 3) / 4), 128, 0, c->st>>>(lo, hi, DP<NodeRec>(c->nodes), box,
+                                                                         DP<H>(c->M), M32);
+        NB_LAUNCHED(c, "m2m");
+    }
+    if (c->timing) cudaEventRecord(c->ev[4], c->st);
+
+    const size_t smem = (size_t)Prec<MODE>::trav_warps * TravSmem<MODE, P>::per_warp;
+    NB_CU(c, cudaFuncSetAttribute(k_traverse<MODE, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        size_t want_pend = (size_t)64 * nn + 1024, want_p2p = (size_t)96 * c->nleaves + 1024;
+        if (c->pend_cap < want_pend) c->pend_cap = want_pend;
+        if (c->p2p_cap < want_p2p) c->p2p_cap = want_p2p;
+        NB_TRY(nb_grow(c, c->pend_list, sizeof(uint32_t) * c->pend_cap));
+        NB_TRY(nb_grow(c, c->p2p_list, sizeof(uint32_t) * c->p2p_cap));
+        if (c->record_m2l) {
+            size_t want_m2l = (size_t)256 * nn + 1024;
+            if (c->m2l_cap < want_m2l) c->m2l_cap = want_m2l;
+            NB_TRY(nb_grow(c, c->m2l_list, sizeof(uint32_t) * c->m2l_cap));
+            NB_TRY(nb_grow(c, c->m2l_off, sizeof(uint32_t) * nn));
+            NB_TRY(nb_grow(c, c->m2l_cnt, sizeof(uint32_t) * nn));
+            NB_CU(c, cudaMemsetAsync(c->m2l_cnt.p, 0, sizeof(uint32_t) * nn, c->st));
+        }
+        int32_t* info = DP<int32_t>(c->info);
+        NB_CU(c, cudaMemsetAsync(info + INFO_PEND_TAIL, 0, 3 * sizeof(int32_t), c->st));
+        NB_CU(c, cudaMemsetAsync(info + INFO_ERR, 0, sizeof(int32_t), c->st));
+        k_root<MODE, P><<<1, 32, 0, c->st>>>(DP<NodeRec>(c->nodes), DP<H>(c->L), DP<uint32_t>(c->pend_off),
+                                             DP<uint32_t>(c->pend_cnt), DP<uint32_t>(c->pend_list),
+                                             DP<uint32_t>(c->p2p_off), DP<uint32_t>(c->p2p_cnt),
+                                             DP<uint32_t>(c->p2p_list), info);
+        NB_LAUNCHED(c, "root");
+        TravArgs A;
+        A.nodes = DP<NodeRec>(c->nodes);
+        A.box = box;
+        A.Mm2l = MODE == NBODY_PREC_MIXED ? (const void*)M32 : (const void*)c->M.p;
+        A.L = c->L.p;
+        A.pend_off = DP<uint32_t>(c->pend_off); A.pend_cnt = DP<uint32_t>(c->pend_cnt);
+        A.pend_list = DP<uint32_t>(c->pend_list);
+        A.p2p_off = DP<uint32_t>(c->p2p_off); A.p2p_cnt = DP<uint32_t>(c->p2p_cnt);
+        A.p2p_list = DP<uint32_t>(c->p2p_list);
+        A.pend_cap = (uint32_t)c->pend_cap; A.p2p_cap = (uint32_t)c->p2p_cap;
+        A.m2l_list = c->record_m2l ? DP<uint32_t>(c->m2l_list) : nullptr;
+        A.m2l_off = c->record_m2l ? DP<uint32_t>(c->m2l_off) : nullptr;
+        A.m2l_cnt = c->record_m2l ? DP<uint32_t>(c->m2l_cnt) : nullptr;
+        A.m2l_cap = (uint32_t)c->m2l_cap;
+        A.info = info;
+        const float th = (float)c->prm.theta;
+        A.theta2x4 = 4.0 * (double)(th * th);
+        A.eps2 = c->prm.eps * c->prm.eps;
+        for (int r = 1; r <= c->depth; ++r) {
+            A.lo = c->level_start[r];
+            A.hi = c->level_start[r + 1];
+            if (A.hi <= A.lo) continue;
+            const int W = Prec<MODE>::trav_warps;
+            k_traverse<MODE, P><<<(unsigned)((A.hi - A.lo + W - 1) / W), 32 * W, smem, c->st>>>(A);
+            NB_LAUNCHED(c, "traverse");
+        }
+        NB_CU(c, cudaMemcpyAsync(c->h_info, info, sizeof(int32_t) * INFO_WORDS, cudaMemcpyDeviceToHost, c->st));
+        NB_CU(c, cudaStreamSynchronize(c->st));
+        const uint32_t e = (uint32_t)c->h_info[INFO_ERR];
+        if (e & NB_ERRBIT_STACK) return nb_fail(c, NBODY_ERR_CAPACITY, "traversal descent stack overflow");
+        if (!(e & (NB_ERRBIT_PEND_CAP | NB_ERRBIT_P2P_CAP | NB_ERRBIT_M2L_CAP))) break;
+        if (e & NB_ERRBIT_M2L_CAP)
+            c->m2l_cap = std::max<size_t>(2 * c->m2l_cap, (size_t)(uint32_t)c->h_info[INFO_M2L_TAIL] + 1024);
+        if (e & NB_ERRBIT_PEND_CAP)
+            c->pend_cap = std::max<size_t>(2 * c->pend_cap, (size_t)(uint32_t)c->h_info[INFO_PEND_TAIL] + 1024);
+        if (e & NB_ERRBIT_P2P_CAP)
+            c->p2p_cap = std::max<size_t>(2 * c->p2p_cap, (size_t)(uint32_t)c->h_info[INFO_P2P_TAIL] + 1024);
+        if (attempt == 7) return nb_fail(c, NBODY_ERR_CAPACITY, "interaction lists kept overflowing");
+    }
+    if (c->timing) cudaEventRecord(c->ev[5], c->st);
+
+    P2PArgs B;
+    B.leaves = DP<uint32_t>(c->leaves);
+    B.nleaves = c->nleaves;
+    B.nodes = DP<NodeRec>(c->nodes);
+    B.box = box;
+    B.src = c->src.p;
+    B.L = c->L.p;
+    B.p2p_off = DP<uint32_t>(c->p2p_off); B.p2p_cnt = DP<uint32_t>(c->p2p_cnt); B.p2p_list = DP<uint32_t>(c->p2p_list);
+    B.x = c->x[cur].p; B.y = c->y[cur].p; B.z = c->z[cur].p;
+    B.vx = c->vx[cur].p; B.vy = c->vy[cur].p; B.vz = c->vz[cur].p;
+    B.ax = c->ax[cur].p; B.ay = c->ay[cur].p; B.az = c->az[cur].p;
+    B.m = c->m[cur].p; B.q = c->q[cur].p;
+    B.pot = want_pot ? c->pot.p : nullptr;
+    B.eps2 = c->prm.eps * c->prm.eps;
+    B.G = c->prm.G;
+    B.dt = c->prm.dt;
+    B.integ = integ;
+    const unsigned g = (unsigned)((c->nleaves + P2P_WARPS - 1) / P2P_WARPS);
+    if (want_pot) k_p2p<MODE, P, true><<<g, 32 * P2P_WARPS, 0, c->st>>>(B);
+    else k_p2p<MODE, P, false><<<g, 32 * P2P_WARPS, 0, c->st>>>(B);
+    NB_LAUNCHED(c, "p2p");
+    if (c->timing) cudaEventRecord(c->ev[6], c->st);
+    return NBODY_OK;
+}
+
+template <int MODE>
+int fmm_dispatch(nbody_ctx* c, int integ, bool want_pot) {
+    switch (c->prm.order) {
+        case 1: return fmm_forces<MODE, 1>(c, integ, want_pot);
+        case 2: return fmm_forces<MODE, 2>(c, integ, want_pot);
+        case 3: return fmm_forces<MODE, 3>(c, integ, want_pot);
+        case 4: return fmm_forces<MODE, 4>(c, integ, want_pot);
+        case 5: return fmm_forces<MODE, 5>(c, integ, want_pot);
+        case 6: return fmm_forces<MODE, 6>(c, integ, want_pot);
+        case 7: return fmm_forces<MODE, 7>(c, integ, want_pot);
+        case 8: return fmm_forces<MODE, 8>(c, integ, want_pot);
+        default: return nb_fail(c, NBODY_ERR_INVALID, "order must be 1..8");
+    }
+}
+
+}  // namespace nbfmm

@@ -1,0 +1,190 @@
+// Internal definitions shared by the CUDA translation units of libnbody_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/nbody_gb300.h"
+
+#define NB_LEVELS 21               // bits per axis of the Morton grid; deepest level
+#define NB_PMAX 8                  // highest expansion order compiled
+#define NB_TMAX 165                // terms at NB_PMAX
+#define NB_WARPS_TRAV 8            // warps per block in the traversal kernel
+
+// error bits raised on the device (ctx->d_info[INFO_ERR])
+#define NB_ERRBIT_PEND_CAP 1u      // refinement list capacity exceeded
+#define NB_ERRBIT_P2P_CAP 2u       // near-field list capacity exceeded
+#define NB_ERRBIT_STACK 4u         // per-warp descent stack overflow
+#define NB_ERRBIT_RANGE 8u         // a particle lay outside a fixed root box
+#define NB_ERRBIT_NONFINITE 16u    // a position was not finite
+#define NB_ERRBIT_M2L_CAP 32u      // recorded far-field list capacity exceeded
+
+// layout of the small device info block (int32 words)
+enum {
+    INFO_ERR = 0,
+    INFO_DEPTH = 1,
+    INFO_NNODES = 2,
+    INFO_NLEAVES = 3,
+    INFO_PEND_TAIL = 4,
+    INFO_P2P_TAIL = 5,
+    INFO_M2L_TAIL = 6,
+    INFO_HIST = 8,                 // 8 .. 8+NB_LEVELS: nodes per level
+    INFO_WORDS = 32
+};
+
+// one octree node, breadth-first order, 32 bytes
+struct __align__(16) NodeRec {
+    uint32_t ix, iy, iz;           // cell coordinates at its level
+    uint32_t begin, count;         // particle range in Morton order
+    int32_t parent;                // -1 for the root
+    int32_t child_begin;           // first child (children are contiguous)
+    uint8_t level, nchild;         // nchild == 0 <=> leaf
+    uint16_t pad;
+};
+static_assert(sizeof(NodeRec) == 32, "NodeRec must stay 32 bytes");
+
+// root box on the device: origin xyz, side, 2^21/side, fine unit side/2^22
+struct BoxDev {
+    double ox, oy, oz, side, scale, unit;
+};
+
+// grow-only device allocation
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct nbody_ctx {
+    nbody_params prm;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    int64_t n = 0;
+    double time = 0.0;
+    bool have_acc = false;
+    size_t rsz = 8;                // bytes of a state scalar (4 in the fp32 form)
+
+    // particle state in Morton order (double buffered across the re-sort)
+    int cur = 0;
+    DevBuf x[2], y[2], z[2], vx[2], vy[2], vz[2], ax[2], ay[2], az[2], m[2], q[2], id[2];
+    DevBuf pot;                    // potential per particle (diagnostics)
+
+    // sort scratch
+    DevBuf keys[2], vals[2], hist, hist_scan, scan_part;
+
+    // tree scratch and result
+    DevBuf cpl, wnd, leaflvl, nc, pfx, seedk[2], seedv[2], nodes, leafflag, leafpfx, leaves;
+    int64_t nnodes = 0, nleaves = 0;
+    int depth = 0;
+    int level_start[NB_LEVELS + 3] = {0};
+
+    // expansions and lists
+    DevBuf M, M32, L, src;
+    DevBuf pend_off, pend_cnt, p2p_off, p2p_cnt, pend_list, p2p_list;
+    size_t pend_cap = 0, p2p_cap = 0;
+    bool record_m2l = false;       // keep the far-field partner lists (inspection only)
+    DevBuf m2l_off, m2l_cnt, m2l_list;
+    size_t m2l_cap = 0;
+    DevBuf stage;                  // host <-> device staging (interleaved doubles)
+    DevBuf diag;
+
+    // small device blocks + pinned mirrors
+    DevBuf info, box, bbox;
+    int32_t* h_info = nullptr;
+    double* h_box = nullptr;
+
+    // per-phase timing
+    bool timing = false;
+    cudaEvent_t ev[16] = {};
+    float phase_ms[16] = {0};
+
+    std::string err;
+};
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+int nb_fail(nbody_ctx* c, int code, const std::string& msg);
+int nb_cuda(nbody_ctx* c, cudaError_t e, const char* what);
+int nb_grow(nbody_ctx* c, DevBuf& b, size_t bytes);
+
+#define NB_TRY(expr)                 \
+    do {                             \
+        int _rc = (expr);            \
+        if (_rc != NBODY_OK) return _rc; \
+    } while (0)
+#define NB_CU(c, expr) NB_TRY(nb_cuda((c), (expr), #expr))
+#define NB_LAUNCHED(c, name) NB_TRY(nb_cuda((c), cudaGetLastError(), name))
+
+template <typename T>
+static inline T* DP(const DevBuf& b) { return reinterpret_cast<T*>(b.p); }
+
+// scan + sort (sort.cu)
+int nb_scan_u32(nbody_ctx* c, const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total_dev);
+int nb_radix_sort(nbody_ctx* c, int64_t n, uint64_t* k0, uint32_t* v0, uint64_t* k1, uint32_t* v1, int begin_bit,
+                  int end_bit, int* result_in_first);
+
+// tree (tree.cu)
+int nb_begin_step(nbody_ctx* c, int kdk);
+int nb_sort_and_gather(nbody_ctx* c);
+int nb_build_tree(nbody_ctx* c);
+
+// fmm (fmm_*.cu)
+int nb_fmm_forces_fp32(nbody_ctx* c, int integ, bool want_pot);
+int nb_fmm_forces_mixed(nbody_ctx* c, int integ, bool want_pot);
+int nb_fmm_forces_fp64(nbody_ctx* c, int integ, bool want_pot);
+
+// integration modes of the force epilogue
+enum { NB_INTEG_NONE = 0, NB_INTEG_KDK_CLOSE = 1, NB_INTEG_EULER = 2 };
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float nb_fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double nb_fma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float nb_rsqrt(float s) { return rsqrtf(s); }
+__device__ __forceinline__ double nb_rsqrt(double s) { return rsqrt(s); }
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t lanemask_lt() { return (1u << lane_id()) - 1u; }
+
+// inclusive warp scan of v
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane_id() >= (uint32_t)o) v += t;
+    }
+    return v;
+}
+
+// 21-bit spread / compact for Morton interleaving (x = bit 0 of each triple)
+__host__ __device__ __forceinline__ uint64_t nb_spread3(uint64_t v) {
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+__host__ __device__ __forceinline__ uint32_t nb_compact3(uint64_t v) {
+    v &= 0x1249249249249249ull;
+    v = (v ^ (v >> 2)) & 0x10c30c30c30c30c3ull;
+    v = (v ^ (v >> 4)) & 0x100f00f00f00f00full;
+    v = (v ^ (v >> 8)) & 0x1f0000ff0000ffull;
+    v = (v ^ (v >> 16)) & 0x1f00000000ffffull;
+    v = (v ^ (v >> 32)) & 0x1fffffull;
+    return (uint32_t)v;
+}
+
+// centre of a node in fine units (side / 2^22): (2 i + 1) << (21 - level)
+__device__ __forceinline__ void nb_centre_fine(const NodeRec& nd, long long& cx, long long& cy, long long& cz) {
+    int sh = NB_LEVELS - nd.level;
+    cx = (2ll * nd.ix + 1) << sh;
+    cy = (2ll * nd.iy + 1) << sh;
+    cz = (2ll * nd.iz + 1) << sh;
+}
+__device__ __forceinline__ long long nb_width_fine(const NodeRec& nd) { return 1ll << (NB_LEVELS + 1 - nd.level); }

@@ -1,0 +1,199 @@
+"""Host-side mirror of the reference's Simulation interface over the C ABI.
+
+The reference exposes ``nbody::Simulation<Scalar, Vector>`` with a
+``Particle{position, velocity, mass, charge}`` record, ``step()`` returning
+the new time and ``particles()`` returning the particles in octree leaf order
+(include/nbody/simulation.h:16-35, src/open_cl_simulation.cpp:53-106).
+``CudaSimulation`` keeps those names, argument meanings and the constructor
+of ``OpenClSimulation(bounds, particles, time_step, log)``
+(include/nbody/open_cl_simulation.h:194-198), and adds array-level calls
+(forces, diagnostics, tree and interaction inspection) for callers that do
+not go through per-particle records.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import INTEG_EULER, INTEG_LEAPFROG, PREC_FP32, PREC_FP64, PREC_MIXED, NbodyError, check, ptr
+
+__all__ = ["Particle", "CudaSimulation", "params", "PREC_FP32", "PREC_MIXED", "PREC_FP64", "INTEG_LEAPFROG",
+           "INTEG_EULER", "NbodyError"]
+
+
+@dataclass
+class Particle:
+    """Same fields as Simulation::Particle (include/nbody/simulation.h:16-32)."""
+    position: Sequence[float]
+    velocity: Sequence[float]
+    mass: float
+    charge: float
+
+
+def params(**kw) -> _lib.Params:
+    """nbody_params with the reference defaults, overridden by keyword."""
+    L = _lib.load()
+    p = _lib.Params()
+    L.nbody_default_params(C.byref(p))
+    for k, v in kw.items():
+        if k == "box_min":
+            p.box_min[0], p.box_min[1], p.box_min[2] = v
+        elif hasattr(p, k):
+            setattr(p, k, v)
+        else:
+            raise TypeError(f"unknown parameter {k}")
+    return p
+
+
+class CudaSimulation:
+    """Drop-in for OpenClSimulation on one GB300.
+
+    CudaSimulation(bounds, particles, time_step, log=None, **params)
+      bounds     extent of the root box [0, bounds) as in the reference
+                 (its fourth component, if given, is ignored)
+      particles  iterable of Particle (or use from_arrays)
+      time_step  dt
+      params     any nbody_params field (precision, order, leaf_capacity,
+                 theta, eps, G, integrator, fixed_box, box_min, box_size, ...)
+    Errors raise NbodyError (the reference raises std::runtime_error /
+    cl::Error, src/open_cl_simulation.cpp:630,648,767).
+    """
+
+    def __init__(self, bounds=None, particles: Iterable[Particle] | None = None, time_step: float = 1e-3,
+                 log=None, **kw):
+        L = _lib.load()
+        if bounds is not None and "box_size" not in kw:
+            kw["box_size"] = float(max(bounds[0], bounds[1], bounds[2]))
+            kw.setdefault("box_min", (0.0, 0.0, 0.0))
+            kw.setdefault("fixed_box", 1)
+        kw.setdefault("dt", time_step)
+        self._p = params(**kw)
+        self._log = log
+        h = C.c_void_p()
+        rc = L.nbody_create(C.byref(self._p), C.byref(h))
+        if rc != 0:
+            raise NbodyError(rc, L.nbody_last_error(None).decode())
+        self._h = h
+        self.n = 0
+        if particles is not None:
+            ps = list(particles)
+            pos = np.array([p.position[:3] for p in ps], dtype=np.float64)
+            vel = np.array([p.velocity[:3] for p in ps], dtype=np.float64)
+            mass = np.array([p.mass for p in ps], dtype=np.float64)
+            charge = np.array([p.charge for p in ps], dtype=np.float64)
+            self.set_state(pos, vel, mass, charge)
+
+    @classmethod
+    def from_arrays(cls, pos, vel=None, mass=None, charge=None, **kw):
+        sim = cls(None, None, kw.pop("dt", 1e-3), **kw)
+        sim.set_state(pos, vel, mass, charge)
+        return sim
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().nbody_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state --------------------------------------------------------------
+    def set_state(self, pos, vel=None, mass=None, charge=None):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        n = pos.shape[0]
+        vel = np.zeros((n, 3)) if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(n, 3)
+        mass = np.ones(n) if mass is None else np.ascontiguousarray(mass, dtype=np.float64).reshape(n)
+        charge = None if charge is None else np.ascontiguousarray(charge, dtype=np.float64).reshape(n)
+        check(self._h, _lib.load().nbody_set_state(self._h, n, ptr(pos), ptr(vel), ptr(mass), ptr(charge)))
+        self.n = n
+
+    def state(self, order: str = "input"):
+        """(pos, vel, mass, charge, ids); order 'input' or 'leaf' (Morton)."""
+        n = self.n
+        pos, vel = np.empty((n, 3)), np.empty((n, 3))
+        mass, charge = np.empty(n), np.empty(n)
+        ids = np.empty(n, np.int64)
+        check(self._h, _lib.load().nbody_get_state(self._h, 1 if order == "input" else 0, ptr(pos), ptr(vel),
+                                                   ptr(mass), ptr(charge), ptr(ids)))
+        return pos, vel, mass, charge, ids
+
+    # -- the reference interface ---------------------------------------------
+    def step(self, nsteps: int = 1) -> float:
+        """Advances nsteps time steps; returns the new time (Simulation::step)."""
+        t = C.c_double()
+        if self._log is not None:
+            self._log.write(f"Starting a new step (t={self.time}).\n")
+        check(self._h, _lib.load().nbody_step(self._h, nsteps, C.byref(t)))
+        return t.value
+
+    def particles(self):
+        """Particles in octree leaf order, as the reference returns them."""
+        pos, vel, mass, charge, _ = self.state("leaf")
+        return [Particle(tuple(pos[i]), tuple(vel[i]), float(mass[i]), float(charge[i])) for i in range(self.n)]
+
+    @property
+    def time(self) -> float:
+        t = C.c_double()
+        check(self._h, _lib.load().nbody_get_time(self._h, C.byref(t)))
+        return t.value
+
+    # -- additions ------------------------------------------------------------
+    def forces(self, potential: bool = False):
+        """Accelerations (n,3) [and potential per unit charge (n,)], input order."""
+        acc = np.empty((self.n, 3))
+        pot = np.empty(self.n) if potential else None
+        check(self._h, _lib.load().nbody_compute_forces(self._h, ptr(acc), ptr(pot)))
+        return (acc, pot) if potential else acc
+
+    def diagnostics(self):
+        out = np.empty(9)
+        check(self._h, _lib.load().nbody_diagnostics(self._h, ptr(out)))
+        return {"kinetic": out[0], "potential": out[1], "energy": out[0] + out[1], "momentum": out[2:5].copy(),
+                "angular_momentum": out[5:8].copy(), "mass": out[8]}
+
+    def tree(self):
+        """(keys, perm, nodes) of the last tree; nodes rows as in the C ABI."""
+        L = _lib.load()
+        n, nn, nl, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int()
+        check(self._h, L.nbody_tree_info(self._h, C.byref(n), C.byref(nn), C.byref(nl), C.byref(d)))
+        keys = np.empty(n.value, np.uint64)
+        perm = np.empty(n.value, np.int64)
+        nodes = np.empty((nn.value, 9), np.int32)
+        check(self._h, L.nbody_get_tree(self._h, ptr(keys), ptr(perm), ptr(nodes)))
+        return keys, perm, nodes
+
+    def interactions(self, which: str):
+        """(target, source) node pairs: which = 'm2l' or 'p2p'."""
+        L = _lib.load()
+        w = 0 if which == "m2l" else 1
+        k = C.c_int64()
+        check(self._h, L.nbody_get_interactions(self._h, w, C.byref(k), None))
+        out = np.empty((max(k.value, 1), 2), np.int32)
+        check(self._h, L.nbody_get_interactions(self._h, w, C.byref(k), ptr(out)))
+        return out[: k.value]
+
+    def set_timing(self, on: bool = True):
+        check(self._h, _lib.load().nbody_set_timing(self._h, int(on)))
+
+    def phase_times(self):
+        out = np.zeros(6, np.float32)
+        check(self._h, _lib.load().nbody_phase_times(self._h, ptr(out), 6))
+        return out
+
+    @property
+    def stream(self) -> int:
+        return _lib.load().nbody_stream(self._h) or 0

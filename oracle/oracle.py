@@ -1,0 +1,290 @@
+"""ctypes binding for the CPU oracle (test infrastructure only).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
+leg import this module, and only as the checker or the timed CPU baseline.
+The product (``nbody_gb300``) never imports it.
+
+``liboracle.so`` is the C restatement in ``nbody_oracle.c``.  ``libnbody_ref.so``
+(``oracle/_ref``) is the reference's own code compiled from its sources; it only
+exists where the reference is mounted and is used to pin the restatement.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_REF = None
+
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+_u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+
+
+def build(ref: bool | None = None) -> None:
+    """Compile liboracle.so (and, if the reference is mounted, libnbody_ref.so)."""
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    if ref is None:
+        ref = os.path.isdir("/root/reference/src")
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = os.path.join(HERE, "_build", "liboracle.so")
+    if not os.path.exists(path):
+        build(ref=False)
+    L = C.CDLL(path)
+    L.orc_create.restype = C.c_void_p
+    L.orc_create.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _f64p, C.c_int, C.c_int]
+    L.orc_destroy.argtypes = [C.c_void_p]
+    L.orc_nnodes.restype = C.c_int64
+    L.orc_nnodes.argtypes = [C.c_void_p]
+    L.orc_depth.restype = C.c_int
+    L.orc_depth.argtypes = [C.c_void_p]
+    L.orc_get_order.argtypes = [C.c_void_p, _u32p, _u64p]
+    L.orc_get_nodes.argtypes = [C.c_void_p, _i32p]
+    L.orc_traverse.argtypes = [C.c_void_p, C.c_double]
+    L.orc_list_size.restype = C.c_int64
+    L.orc_list_size.argtypes = [C.c_void_p, C.c_int]
+    L.orc_get_list.argtypes = [C.c_void_p, C.c_int, _i32p]
+    L.orc_fmm.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, _f64p, _f64p, C.c_void_p, C.c_void_p]
+    L.orc_ref_forces_f32.argtypes = [C.c_void_p, C.c_float, _f32p, _f32p]
+    L.orc_direct.argtypes = [C.c_int64, _f64p, _f64p, _f64p, C.c_double, C.c_double, C.c_int64, C.c_void_p,
+                             _f64p, C.c_void_p, C.c_int]
+    L.orc_leapfrog.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _f64p, C.c_double, C.c_double, C.c_double,
+                               C.c_int, _f64p, C.c_int, C.c_int]
+    L.orc_naive_steps.restype = C.c_float
+    L.orc_naive_steps.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_float, C.c_int, C.c_int]
+    L.orc_naive_kick_mt.restype = C.c_int64
+    L.orc_naive_kick_mt.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_float, C.c_int, C.c_int,
+                                    C.c_int, C.c_int]
+    L.orc_morton_keys.argtypes = [C.c_int64, _f64p, _f64p, _u64p]
+    L.orc_derivs.argtypes = [C.c_int, _f64p, C.c_double, _f64p]
+    L.orc_nterms.restype = C.c_int
+    L.orc_nterms.argtypes = [C.c_int]
+    _LIB = L
+    return L
+
+
+def ref_lib():
+    """The reference's own code compiled here, or None where it was not built."""
+    global _REF
+    if _REF is not None:
+        return _REF
+    path = os.path.join(HERE, "_ref", "libnbody_ref.so")
+    if not os.path.exists(path):
+        return None
+    try:
+        R = C.CDLL(path)
+    except OSError:
+        return None
+    R.ref_naive_steps.restype = C.c_float
+    R.ref_naive_steps.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_float, C.c_int]
+    R.ref_fmm_run.restype = C.c_int
+    R.ref_fmm_run.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, _i32p, _f64p, C.c_float, C.c_int,
+                              C.POINTER(C.c_int), _i32p, C.POINTER(C.c_int), _i32p, _f32p, _f32p, _f32p, _f32p]
+    _REF = R
+    return R
+
+
+NODE_FIELDS = ("level", "ix", "iy", "iz", "begin", "count", "parent", "child_begin", "nchild")
+
+
+def theta2_f32(theta: float) -> float:
+    """theta^2 as the reference forms it in single precision (src/interaction.cl:78)."""
+    t = np.float32(theta)
+    return float(np.float32(t * t))
+
+
+class Tree:
+    """Sorted particles + breadth-first octree + interaction lists (oracle)."""
+
+    def __init__(self, pos, q=None, m=None, box=None, cap=16, maxlevel=21):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        n = pos.shape[0]
+        self.n = n
+        q = np.ones(n) if q is None else np.ascontiguousarray(q, dtype=np.float64)
+        m = q.copy() if m is None else np.ascontiguousarray(m, dtype=np.float64)
+        if box is None:
+            box = bounding_box(pos)
+        self.box = np.ascontiguousarray(box, dtype=np.float64)
+        L = lib()
+        self._h = L.orc_create(n, pos.reshape(-1), q, m, self.box, cap, maxlevel)
+        self.nnodes = L.orc_nnodes(self._h)
+        self.depth = L.orc_depth(self._h)
+        self.perm = np.zeros(max(n, 1), np.uint32)
+        self.keys = np.zeros(max(n, 1), np.uint64)
+        L.orc_get_order(self._h, self.perm, self.keys)
+        self.perm, self.keys = self.perm[:n], self.keys[:n]
+        nodes = np.zeros((self.nnodes, 9), np.int32)
+        L.orc_get_nodes(self._h, nodes)
+        self.nodes = nodes
+        self._lists = None
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_destroy(self._h)
+            self._h = None
+
+    def field(self, name):
+        return self.nodes[:, NODE_FIELDS.index(name)]
+
+    def traverse(self, theta=0.5):
+        lib().orc_traverse(self._h, theta2_f32(theta))
+        self._lists = {}
+        return self
+
+    def pairs(self, which):
+        """which in {'m2l','p2p','pend'}: int32 (k, 2) rows (target, source)."""
+        w = {"m2l": 0, "p2p": 1, "pend": 2}[which]
+        L = lib()
+        k = L.orc_list_size(self._h, w)
+        out = np.zeros((max(k, 1), 2), np.int32)
+        L.orc_get_list(self._h, w, out)
+        return out[:k]
+
+    def fmm(self, order, eps, G=1.0):
+        acc = np.zeros(3 * max(self.n, 1))
+        pot = np.zeros(max(self.n, 1))
+        rc = lib().orc_fmm(self._h, order, eps, G, acc, pot, None, None)
+        if rc != 0:
+            raise RuntimeError("orc_fmm failed (traverse first; order in 1..10)")
+        return acc[: 3 * self.n].reshape(-1, 3), pot[: self.n]
+
+    def ref_forces_f32(self, eps=0.01):
+        fl = np.zeros(3 * max(self.n, 1), np.float32)
+        fn = np.zeros(3 * max(self.n, 1), np.float32)
+        lib().orc_ref_forces_f32(self._h, eps, fl, fn)
+        return fl[: 3 * self.n].reshape(-1, 3), fn[: 3 * self.n].reshape(-1, 3)
+
+
+def bounding_box(pos):
+    """Power-of-two cube enclosing pos, origin on a multiple of side/2.
+
+    Same rule as the device (data-bounding root box): side = smallest power of
+    two >= (max extent) * (1 + 2^-20), origin = floor(min / (side/2)) * (side/2),
+    and doubled until the box covers every particle.
+    """
+    pos = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
+    if pos.shape[0] == 0:
+        return np.array([0.0, 0.0, 0.0, 1.0])
+    lo, hi = pos.min(axis=0), pos.max(axis=0)
+    ext = float((hi - lo).max()) * (1.0 + 2.0 ** -20)
+    side = 1.0
+    while side < ext:
+        side *= 2.0
+    while side * 0.5 >= ext and ext > 0:
+        side *= 0.5
+    while True:
+        half = side / 2.0
+        origin = np.floor(lo / half) * half
+        if np.all(origin + side > hi):
+            return np.array([origin[0], origin[1], origin[2], side])
+        side *= 2.0
+
+
+def direct(pos, q=None, m=None, eps=0.01, G=1.0, targets=None, nthreads=None):
+    """FP64 softened direct sum: (acc, pot) for the targets (default all)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    n = pos.shape[0]
+    q = np.ones(n) if q is None else np.ascontiguousarray(q, dtype=np.float64)
+    m = q.copy() if m is None else np.ascontiguousarray(m, dtype=np.float64)
+    nthreads = nthreads or min(os.cpu_count() or 1, 32)
+    if targets is None:
+        nt, tp = n, None
+        tgt = None
+    else:
+        tgt = np.ascontiguousarray(targets, dtype=np.int64)
+        nt, tp = tgt.shape[0], tgt.ctypes.data
+    acc = np.zeros(3 * max(nt, 1))
+    pot = np.zeros(max(nt, 1))
+    lib().orc_direct(n, pos.reshape(-1), q, m, eps, G, nt, tp, acc, pot.ctypes.data, nthreads)
+    return acc[: 3 * nt].reshape(-1, 3), pot[:nt]
+
+
+def leapfrog(pos, vel, q, m, eps, G, dt, steps, nthreads=None):
+    """FP64 direct-sum kick-drift-kick leapfrog; returns (pos, vel, acc)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1).copy()
+    vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1).copy()
+    n = pos.shape[0] // 3
+    acc = np.zeros(3 * n)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    m = np.ascontiguousarray(m, dtype=np.float64)
+    lib().orc_leapfrog(n, pos, vel, q, m, eps, G, dt, steps, acc, 0, nthreads or min(os.cpu_count() or 1, 32))
+    return pos.reshape(-1, 3), vel.reshape(-1, 3), acc.reshape(-1, 3)
+
+
+def naive_steps(pos4, vel4, mass, charge, G, dt, steps, fix_delta=False):
+    """Port of the reference CPU path (src/naive_simulation.cpp:7-46)."""
+    p = np.ascontiguousarray(pos4, dtype=np.float32).copy()
+    v = np.ascontiguousarray(vel4, dtype=np.float32).copy()
+    t = lib().orc_naive_steps(p.shape[0], p.reshape(-1), v.reshape(-1), np.ascontiguousarray(mass, np.float32),
+                              np.ascontiguousarray(charge, np.float32), G, dt, steps, int(fix_delta))
+    return p, v, t
+
+
+def ref_naive_steps(pos4, vel4, mass, charge, G, dt, steps):
+    """The reference's own src/naive_simulation.cpp (only where it was built)."""
+    R = ref_lib()
+    if R is None:
+        return None
+    p = np.ascontiguousarray(pos4, dtype=np.float32).copy()
+    v = np.ascontiguousarray(vel4, dtype=np.float32).copy()
+    t = R.ref_naive_steps(p.shape[0], p.reshape(-1), v.reshape(-1), np.ascontiguousarray(mass, np.float32),
+                          np.ascontiguousarray(charge, np.float32), G, dt, steps)
+    return p, v, t
+
+
+def ref_fmm_run(pos_sorted, vel_sorted, mass_sorted, charge_sorted, nodes, box, dt):
+    """Run the reference's FMM kernels (src/*.cl) on the CPU over a given tree.
+
+    Inputs are in sorted (leaf) order, float32.  Returns dict with leaf/node
+    interaction pairs (breadth-first node ids), per-particle leaf and node
+    forces and the explicit-Euler-stepped state, all in sorted order.
+    """
+    R = ref_lib()
+    if R is None:
+        return None
+    n = pos_sorted.shape[0]
+    cap = 8 * 1024 * 1024
+    lp = np.zeros(2 * cap, np.int32)
+    npairs = np.zeros(2 * cap, np.int32)
+    nl, nn = C.c_int(0), C.c_int(0)
+    fl = np.zeros(3 * n, np.float32)
+    fn = np.zeros(3 * n, np.float32)
+    po = np.zeros(3 * n, np.float32)
+    vo = np.zeros(3 * n, np.float32)
+    rc = R.ref_fmm_run(n, np.ascontiguousarray(pos_sorted, np.float32).reshape(-1),
+                       np.ascontiguousarray(vel_sorted, np.float32).reshape(-1),
+                       np.ascontiguousarray(mass_sorted, np.float32), np.ascontiguousarray(charge_sorted, np.float32),
+                       nodes.shape[0], np.ascontiguousarray(nodes, np.int32).reshape(-1),
+                       np.ascontiguousarray(box, np.float64), dt, cap, C.byref(nl), lp, C.byref(nn), npairs,
+                       fl, fn, po, vo)
+    if rc != 0:
+        raise RuntimeError(f"ref_fmm_run failed rc={rc}")
+    return {
+        "leaf_pairs": lp[: 2 * nl.value].reshape(-1, 2).copy(),
+        "node_pairs": npairs[: 2 * nn.value].reshape(-1, 2).copy(),
+        "f_leaf": fl.reshape(-1, 3), "f_node": fn.reshape(-1, 3),
+        "pos": po.reshape(-1, 3), "vel": vo.reshape(-1, 3),
+    }
+
+
+def both_orientations(pairs):
+    """Unordered (a, b) pairs -> set of ordered (t, s) tuples in both directions."""
+    s = set()
+    for a, b in np.asarray(pairs).tolist():
+        s.add((a, b))
+        s.add((b, a))
+    return s
