@@ -1,0 +1,325 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 FMM step: particle-steps/s at N = 1,048,576.
+
+Workload (default): two Plummer spheres of 524,288 bodies colliding
+(eps 0.005, dt 5e-4, theta 0.5, leapfrog), mixed precision, Cartesian order 7
+(the lowest order whose rms force error vs the FP64 direct sum is <= 1e-4 on
+this workload; the error is measured and reported in every run).
+
+  value     device-timed particle-steps/s with the state resident in HBM
+  e2e       the same through the C ABI with host buffers: every step uploads
+            pos/vel/mass/charge/acc from pinned host memory, steps, and reads
+            pos/vel/acc back
+  roofline  the dominant kernel's achieved FP32 throughput (counted flops of
+            the work it did / its CUDA-event time) against the FP32 FMA peak
+            measured on this GPU
+  cpu_baseline  the reference CPU path (a port of src/naive_simulation.cpp),
+            one core, on a bounded row sample of the same N=1M step
+
+--impl reference times the reference's CPU path on all host cores (the
+port, parallel over targets) on the same workload and prints the same line.
+Under torchrun each rank runs an independent replica on its own GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s at N=1M (fwd; fwd+adjoint) at fixed rms force err vs FP64 direct"
+UNIT = "particle-steps/s"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_desc(a):
+    return {
+        "workload": f"collision1m: N={a.n:,} two Plummer spheres (a=1, M=0.5 each, 10a apart on x, impact 1a, "
+                    f"relative speed 0.5), eps={a.eps}, dt={a.dt}, theta={a.theta}, leapfrog KDK",
+        "precision": a.precision, "order": a.order, "leaf_capacity": a.cap,
+        "l2": "working set (state double-buffered + tree + expansions + lists) is several x the 129 MB L2; "
+              "no flush needed",
+        "parallelism": "replicas" if a.gpus > 1 else "single GPU",
+    }
+
+
+class ClockSampler:
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def reference_arm(a, rank, world):
+    """The reference CPU path (port of src/naive_simulation.cpp) on all host cores."""
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from nbody_gb300 import ics
+    L = oracle.lib()
+    pos, vel, m = ics.collision(a.n, seed=a.seed)
+    p4 = np.zeros((a.n, 4), np.float32)
+    p4[:, :3] = pos
+    v4 = np.zeros((a.n, 4), np.float32)
+    v4[:, :3] = vel
+    mf = m.astype(np.float32)
+    cores = os.cpu_count() or 1
+    k = a.ref_targets
+    rng = np.random.default_rng(1)
+    times = []
+    for s in range(a.warmup + a.steps):
+        t0 = int(rng.integers(0, a.n - k))
+        st = time.perf_counter()
+        pairs = L.orc_naive_kick_mt(a.n, p4.reshape(-1), v4.reshape(-1), mf, mf, 1.0, a.dt, t0, t0 + k, 0, cores)
+        el = time.perf_counter() - st
+        if s >= a.warmup:
+            times.append(el / pairs)
+    t_pair = float(np.mean(times))
+    value = 1.0 / ((a.n - 1) * t_pair)          # N / (N (N-1) t_pair)
+    sample = (f"port of src/naive_simulation.cpp per-pair arithmetic (delta bug kept), parallel over targets on "
+              f"{cores} threads: {k} targets x {a.n - 1} sources per step, extrapolated to the full N(N-1) "
+              f"ordered pairs of one N={a.n:,} step")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * a.n / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded), same initial conditions as the GPU arm",
+            "config": workload_desc(a), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def cpu_baseline(a):
+    """One core, serial port of the reference loop, on a bounded row sample of the N=1M step."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from nbody_gb300 import ics
+    L = oracle.lib()
+    pos, vel, m = ics.collision(a.n, seed=a.seed)
+    p4 = np.zeros((a.n, 4), np.float32)
+    p4[:, :3] = pos
+    v4 = np.zeros((a.n, 4), np.float32)
+    v4[:, :3] = vel
+    mf = m.astype(np.float32)
+    rows = 64
+    i1 = a.n
+    pairs = 0
+    st = time.perf_counter()
+    while time.perf_counter() - st < a.cpu_seconds and i1 - rows > 1:
+        pairs += L.orc_naive_rows(a.n, p4.reshape(-1), v4.reshape(-1), mf, mf, 1.0, a.dt, i1 - rows, i1, 0)
+        i1 -= rows
+    el = time.perf_counter() - st
+    t_pair = el / max(pairs, 1)
+    step = 0.5 * a.n * (a.n - 1) * t_pair
+    return {"value": a.n / step, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"serial port of src/naive_simulation.cpp:8-40 (same loop order and arithmetic), rows "
+                      f"[{i1}, {a.n}) of the N={a.n:,} triangle ({pairs:,} pairs, {el:.1f} s), scaled to the "
+                      f"N(N-1)/2 pairs of one step"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1048576)
+    ap.add_argument("--order", type=int, default=7)
+    ap.add_argument("--cap", type=int, default=32)
+    ap.add_argument("--precision", default="mixed", choices=["fp32", "mixed", "fp64"])
+    ap.add_argument("--theta", type=float, default=0.5)
+    ap.add_argument("--eps", type=float, default=0.005)
+    ap.add_argument("--dt", type=float, default=5e-4)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--err-targets", type=int, default=4096)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-targets", type=int, default=1024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    a = ap.parse_args()
+    assert a.warmup >= 0 and a.steps >= 1
+    rank, world, local = dist_env()
+    if a.impl == "reference":
+        return reference_arm(a, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import nbody_gb300 as nb
+    from nbody_gb300 import _lib, ics
+
+    prec = {"fp32": nb.PREC_FP32, "mixed": nb.PREC_MIXED, "fp64": nb.PREC_FP64}[a.precision]
+    pos, vel, m = ics.collision(a.n, seed=a.seed + rank)
+    sim = nb.CudaSimulation.from_arrays(pos, vel, m, m, precision=prec, order=a.order, leaf_capacity=a.cap,
+                                        theta=a.theta, eps=a.eps, dt=a.dt, integrator=nb.INTEG_LEAPFROG,
+                                        fixed_box=0, device=local)
+    stream = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
+
+    for _ in range(a.warmup):
+        sim.step(1)
+
+    # accuracy at the current state: rms relative force error vs the FP64 direct sum
+    acc = sim.forces()
+    tg = np.random.default_rng(123).choice(a.n, min(a.err_targets, a.n), replace=False)
+    ad, _ = sim.direct(tg)
+    err = np.linalg.norm(acc[tg] - ad, axis=1) / np.linalg.norm(ad, axis=1)
+    rms_err, max_err = float(np.sqrt(np.mean(err ** 2))), float(err.max())
+
+    # timed region: K steps, state resident in HBM, per-phase CUDA events on the library's stream
+    sim.set_timing(True)
+    phases = np.zeros(6)
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    w0 = time.perf_counter()
+    stats = None
+    for _ in range(a.steps):
+        sim.step(1)
+        phases += sim.phase_times()
+        stats = sim.stats()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    clk = clocks.stop()
+    sim.set_timing(False)
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = a.n * a.steps * world / (ms * 1e-3)
+
+    # end to end through the C ABI with pinned host buffers
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    hp, hv, ha = pin((a.n, 3)), pin((a.n, 3)), pin((a.n, 3))
+    hm, hq = pin((a.n,)), pin((a.n,))
+    pos_now, vel_now, m_now, q_now, _, acc_now = sim.state("input", with_acc=True)
+    hp[:], hv[:], ha[:], hm[:], hq[:] = pos_now, vel_now, acc_now, m_now, q_now
+    L = _lib.load()
+    ptr = _lib.ptr
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    e0 = time.perf_counter()
+    for _ in range(a.e2e_steps):
+        _lib.check(sim._h, L.nbody_set_state(sim._h, a.n, ptr(hp), ptr(hv), ptr(hm), ptr(hq), ptr(ha)))
+        _lib.check(sim._h, L.nbody_step(sim._h, 1, None))
+        _lib.check(sim._h, L.nbody_get_state(sim._h, 1, ptr(hp), ptr(hv), None, None, None, ptr(ha)))
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - e0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = a.n * a.e2e_steps * world / e2e_s
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    # roofline of the dominant kernel (per step: one near-field launch; one traversal launch per level)
+    peaks = np.zeros(2)
+    L.nbody_measure_peaks(local, ptr(peaks))
+    fp32_peak_tf = peaks[0] / 1e3
+    per_step = phases / a.steps
+    p2p_flops = stats["p2p_particle_pairs"] * L.nbody_flops_per_p2p()
+    m2l_flops = stats["m2l_pairs"] * L.nbody_flops_per_m2l(a.order)
+    p2p_tf = p2p_flops / (per_step[5] * 1e-3) / 1e12 if per_step[5] > 0 else 0.0
+    trav_tf = m2l_flops / (per_step[4] * 1e-3) / 1e12 if per_step[4] > 0 else 0.0
+    kernels = {
+        "p2p_l2p_integrate": {"ms": per_step[5], "tflops": p2p_tf, "flops_per_launch": p2p_flops, "launches": 1},
+        "traverse_m2l_l2l": {"ms": per_step[4], "tflops": trav_tf, "flops_per_step": m2l_flops,
+                             "launches": stats["depth"]},
+    }
+    dom = "traverse_m2l_l2l" if per_step[4] >= per_step[5] else "p2p_l2p_integrate"
+    ach = kernels[dom]["tflops"]
+    roofline = {"bound": "fp32-pipe", "achieved": ach, "peak": fp32_peak_tf, "unit": "TFLOP/s",
+                "frac": ach / fp32_peak_tf if fp32_peak_tf else None, "traffic": None, "kernel": dom,
+                "peak_source": "FP32 FMA-chain microbenchmark on this GPU (nbody_measure_peaks); "
+                               "MEASURED_PEAKS.json holds HBM and bf16 tensor peaks only",
+                "fp64_peak_tflops_measured": peaks[1] / 1e3,
+                "kernels": kernels,
+                "note": "achieved = counted flops of the work the kernel did (near field: 20 per particle pair; "
+                        "far field: operator flops per cell pair at this order) / CUDA-event time; traffic "
+                        "from ncu in profiles/"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if a.precision == "mixed" else ("f32" if a.precision == "fp32" else "f64"),
+        "data": f"synthetic seeded collision ICs (seed {a.seed} + rank)", "config": workload_desc(a),
+        "rms_force_err_vs_fp64_direct": rms_err, "max_force_err_vs_fp64_direct": max_err,
+        "err_targets": int(len(tg)), "fwd_adjoint": None,
+        "phase_ms_per_step": {k: float(v) for k, v in zip(
+            ["kick_drift_keys", "sort_gather", "tree", "upward", "traverse_m2l_l2l", "p2p_l2p_integrate"], per_step)},
+        "work_per_step": stats, "wall_s_timed": wall,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": a.n * 8 * 11, "d2h_bytes_per_step": a.n * 8 * 9,
+                "steps": a.e2e_steps},
+        "gpu_launches": int(stats["launches"] * a.steps),
+        "clocks": clk, "roofline": roofline,
+    }
+    if world == 1 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(a)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -74,18 +74,21 @@ int nbody_create(const nbody_params* p, nbody_ctx** out);
 /* Releases every device resource of the context. */
 int nbody_destroy(nbody_ctx* c);
 
-/* Uploads particles; arrays are n x 3 (pos, vel) and n (mass, charge);
-   charge may be NULL (charge = mass).  Replaces the particle packing and
-   octree construction of the OpenClSimulation constructor
-   (src/open_cl_simulation.cpp:15-51). Resets the time to 0. */
+/* Uploads particles; arrays are n x 3 (pos, vel, acc) and n (mass, charge);
+   vel and charge may be NULL (zero velocity, charge = mass).  acc, if not
+   NULL, are the accelerations at these positions (as returned by
+   nbody_get_state), which lets a leapfrog run resume without an extra force
+   evaluation.  Replaces the particle packing and octree construction of the
+   OpenClSimulation constructor (src/open_cl_simulation.cpp:15-51). */
 int nbody_set_state(nbody_ctx* c, int64_t n, const double* pos, const double* vel, const double* mass,
-                    const double* charge);
+                    const double* charge, const double* acc);
 
 /* Downloads the state.  order = 0: current Morton (leaf) order, the order
    the reference's particles() returns (src/open_cl_simulation.cpp:53-68);
    order = 1: input order.  Any pointer may be NULL.  ids receives, per row,
-   the input index of that particle. */
-int nbody_get_state(nbody_ctx* c, int order, double* pos, double* vel, double* mass, double* charge, int64_t* ids);
+   the input index of that particle; acc the last accelerations. */
+int nbody_get_state(nbody_ctx* c, int order, double* pos, double* vel, double* mass, double* charge, int64_t* ids,
+                    double* acc);
 
 /* Advances nsteps steps of dt (replaces OpenClSimulation::step,
    src/open_cl_simulation.cpp:70-106); *t_out (may be NULL) receives the
@@ -102,6 +105,29 @@ int nbody_compute_forces(nbody_ctx* c, double* acc, double* pot);
    potential energy, out[2..4] momentum, out[5..7] angular momentum,
    out[8] total mass.  (The reference computes none.) */
 int nbody_diagnostics(nbody_ctx* c, double* out);
+
+/* FP64 softened direct sum at the current positions for nt targets (input
+   indices), on the device: acc (nt x 3) and pot (nt, may be NULL).  The
+   accuracy reference for the FMM (there is no such call in the reference;
+   its CPU path src/naive_simulation.cpp is a direct sum without softening). */
+int nbody_direct_forces(nbody_ctx* c, int64_t nt, const int64_t* targets, double* acc, double* pot);
+
+/* Work counters of the last force evaluation: out[0] far-field (M2L)
+   cell pairs, out[1] near-field particle pairs, out[2] near-field leaf
+   pairs, out[3] nodes, out[4] leaves, out[5] depth, out[6] kernel launches
+   of the last step.  n = number of entries wanted (<= 7). */
+int nbody_get_stats(nbody_ctx* c, int64_t* out, int n);
+
+/* Floating-point operations this build counts per far-field cell pair
+   (derivative tensor + contraction, FMA = 2) and per near-field particle
+   pair (20, the GPU Gems 3 ch. 31 convention) at expansion order p. */
+int64_t nbody_flops_per_m2l(int order);
+int64_t nbody_flops_per_p2p(void);
+
+/* Measured FMA throughput of this device: out[0] FP32 and out[1] FP64
+   GFLOP/s (FMA = 2 flops), from a register-resident FMA chain kernel
+   timed with CUDA events. */
+int nbody_measure_peaks(int device, double* out);
 
 /* Number of particles, nodes, leaves and the depth of the last tree. */
 int nbody_tree_info(nbody_ctx* c, int64_t* n, int64_t* nnodes, int64_t* nleaves, int* depth);

@@ -24,7 +24,8 @@ INTEG_LEAPFROG, INTEG_EULER = 0, 1
 EXPORTS = ("nbody_default_params", "nbody_create", "nbody_destroy", "nbody_set_state", "nbody_get_state",
            "nbody_step", "nbody_compute_forces", "nbody_diagnostics", "nbody_tree_info", "nbody_get_tree",
            "nbody_get_interactions", "nbody_set_timing", "nbody_phase_times", "nbody_stream", "nbody_get_time",
-           "nbody_last_error")
+           "nbody_last_error", "nbody_direct_forces", "nbody_get_stats", "nbody_flops_per_m2l", "nbody_flops_per_p2p",
+           "nbody_measure_peaks")
 
 
 class Params(C.Structure):
@@ -59,8 +60,15 @@ def load(path: str | None = None):
     L.nbody_default_params.restype = None
     L.nbody_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
     L.nbody_destroy.argtypes = [vp]
-    L.nbody_set_state.argtypes = [vp, C.c_int64, vp, vp, vp, vp]
-    L.nbody_get_state.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp]
+    L.nbody_set_state.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp]
+    L.nbody_get_state.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp]
+    L.nbody_direct_forces.argtypes = [vp, C.c_int64, vp, vp, vp]
+    L.nbody_get_stats.argtypes = [vp, vp, C.c_int]
+    L.nbody_flops_per_m2l.argtypes = [C.c_int]
+    L.nbody_flops_per_m2l.restype = C.c_int64
+    L.nbody_flops_per_p2p.argtypes = []
+    L.nbody_flops_per_p2p.restype = C.c_int64
+    L.nbody_measure_peaks.argtypes = [C.c_int, vp]
     L.nbody_step.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
     L.nbody_compute_forces.argtypes = [vp, vp, vp]
     L.nbody_diagnostics.argtypes = [vp, vp]
@@ -76,7 +84,8 @@ def load(path: str | None = None):
     L.nbody_last_error.argtypes = [vp]
     L.nbody_last_error.restype = C.c_char_p
     for name in EXPORTS:
-        if name not in ("nbody_default_params", "nbody_stream", "nbody_last_error"):
+        if name not in ("nbody_default_params", "nbody_stream", "nbody_last_error", "nbody_flops_per_m2l",
+                        "nbody_flops_per_p2p"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L

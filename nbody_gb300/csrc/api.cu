@@ -59,7 +59,7 @@ inline unsigned nblk(int64_t n) { return (unsigned)((n + TB - 1) / TB); }
 
 template <typename R>
 __global__ void k_upload(int64_t n, const double* __restrict__ st, R* x, R* y, R* z, R* vx, R* vy, R* vz, R* ax,
-                         R* ay, R* az, R* m, R* q, uint32_t* id, int have_charge) {
+                         R* ay, R* az, R* m, R* q, uint32_t* id, int have_charge, int have_acc) {
     int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x;
     if (i >= n) return;
     const double* pos = st;
@@ -68,7 +68,12 @@ __global__ void k_upload(int64_t n, const double* __restrict__ st, R* x, R* y, R
     const double* cs = st + 7 * n;
     x[i] = (R)pos[3 * i]; y[i] = (R)pos[3 * i + 1]; z[i] = (R)pos[3 * i + 2];
     vx[i] = (R)vel[3 * i]; vy[i] = (R)vel[3 * i + 1]; vz[i] = (R)vel[3 * i + 2];
-    ax[i] = 0; ay[i] = 0; az[i] = 0;
+    if (have_acc) {
+        const double* ac = st + 9 * n;
+        ax[i] = (R)ac[3 * i]; ay[i] = (R)ac[3 * i + 1]; az[i] = (R)ac[3 * i + 2];
+    } else {
+        ax[i] = 0; ay[i] = 0; az[i] = 0;
+    }
     m[i] = (R)ms[i];
     q[i] = (R)(have_charge ? cs[i] : ms[i]);
     id[i] = (uint32_t)i;
@@ -170,6 +175,7 @@ int fmm(nbody_ctx* c, int integ, bool want_pot) {
 
 // one force evaluation at the current positions, with an optional integrator epilogue
 int evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
+    c->launches = 0;
     if (c->timing) cudaEventRecord(c->ev[0], c->st);
     NB_TRY(nb_begin_step(c, kdk));
     if (c->timing) cudaEventRecord(c->ev[1], c->st);
@@ -177,8 +183,6 @@ int evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
     if (c->timing) cudaEventRecord(c->ev[2], c->st);
     NB_TRY(nb_build_tree(c));
     NB_TRY(fmm(c, integ, want_pot));
-    uint32_t e = (uint32_t)c->h_info[INFO_ERR];
-    if (e & NB_ERRBIT_NONFINITE) return nb_fail(c, NBODY_ERR_STATE, "non-finite particle position");
     if (c->timing) {
         NB_CU(c, cudaEventSynchronize(c->ev[6]));
         for (int i = 0; i < 6; ++i) cudaEventElapsedTime(&c->phase_ms[i], c->ev[i], c->ev[i + 1]);
@@ -274,7 +278,8 @@ int nbody_destroy(nbody_ctx* c) {
         for (DevBuf* b : {&c->x[k], &c->y[k], &c->z[k], &c->vx[k], &c->vy[k], &c->vz[k], &c->ax[k], &c->ay[k], &c->az[k],
                           &c->m[k], &c->q[k], &c->id[k], &c->keys[k], &c->vals[k], &c->seedk[k], &c->seedv[k]})
             release(*b);
-    for (DevBuf* b : {&c->pot, &c->hist, &c->hist_scan, &c->scan_part, &c->cpl, &c->wnd, &c->leaflvl, &c->nc, &c->pfx,
+    for (DevBuf* b : {&c->pot, &c->stats, &c->p2p_nch, &c->p2p_work_off, &c->p2p_psize, &c->p2p_part_off,
+                      &c->p2p_part, &c->hist, &c->hist_scan, &c->scan_part, &c->cpl, &c->wnd, &c->leaflvl, &c->nc, &c->pfx,
                       &c->nodes, &c->leafflag, &c->leafpfx, &c->leaves, &c->M, &c->M32, &c->L, &c->src, &c->pend_off,
                       &c->pend_cnt, &c->p2p_off, &c->p2p_cnt, &c->pend_list, &c->p2p_list, &c->m2l_off, &c->m2l_cnt,
                       &c->m2l_list, &c->stage, &c->diag, &c->info, &c->box, &c->bbox})
@@ -288,7 +293,7 @@ int nbody_destroy(nbody_ctx* c) {
 }
 
 int nbody_set_state(nbody_ctx* c, int64_t n, const double* pos, const double* vel, const double* mass,
-                    const double* charge) {
+                    const double* charge, const double* acc) {
     if (!c) return NBODY_ERR_INVALID;
     if (n < 1 || n > (int64_t)0x7fffffff) return nb_fail(c, NBODY_ERR_INVALID, "n must be in 1..2^31-1");
     if (!pos || !mass) return nb_fail(c, NBODY_ERR_INVALID, "pos and mass are required");
@@ -302,23 +307,24 @@ int nbody_set_state(nbody_ctx* c, int64_t n, const double* pos, const double* ve
     else NB_CU(c, cudaMemsetAsync(st + 3 * n, 0, sizeof(double) * 3 * n, c->st));
     NB_CU(c, cudaMemcpyAsync(st + 6 * n, mass, sizeof(double) * n, cudaMemcpyHostToDevice, c->st));
     if (charge) NB_CU(c, cudaMemcpyAsync(st + 7 * n, charge, sizeof(double) * n, cudaMemcpyHostToDevice, c->st));
+    if (acc) NB_CU(c, cudaMemcpyAsync(st + 9 * n, acc, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->st));
     const int k = 0;
     if (c->rsz == 4)
         k_upload<float><<<nblk(n), TB, 0, c->st>>>(n, st, DP<float>(c->x[k]), DP<float>(c->y[k]), DP<float>(c->z[k]),
                                                    DP<float>(c->vx[k]), DP<float>(c->vy[k]), DP<float>(c->vz[k]),
                                                    DP<float>(c->ax[k]), DP<float>(c->ay[k]), DP<float>(c->az[k]),
                                                    DP<float>(c->m[k]), DP<float>(c->q[k]), DP<uint32_t>(c->id[k]),
-                                                   charge != nullptr);
+                                                   charge != nullptr, acc != nullptr);
     else
         k_upload<double><<<nblk(n), TB, 0, c->st>>>(n, st, DP<double>(c->x[k]), DP<double>(c->y[k]),
                                                     DP<double>(c->z[k]), DP<double>(c->vx[k]), DP<double>(c->vy[k]),
                                                     DP<double>(c->vz[k]), DP<double>(c->ax[k]), DP<double>(c->ay[k]),
                                                     DP<double>(c->az[k]), DP<double>(c->m[k]), DP<double>(c->q[k]),
-                                                    DP<uint32_t>(c->id[k]), charge != nullptr);
+                                                    DP<uint32_t>(c->id[k]), charge != nullptr, acc != nullptr);
     NB_LAUNCHED(c, "upload");
     NB_CU(c, cudaStreamSynchronize(c->st));
     c->time = 0.0;
-    c->have_acc = false;
+    c->have_acc = acc != nullptr;
     return NBODY_OK;
 }
 
@@ -327,7 +333,8 @@ static int fetch(nbody_ctx* c, int order) {
     return c->rsz == 4 ? download_t<float>(c, order) : download_t<double>(c, order);
 }
 
-int nbody_get_state(nbody_ctx* c, int order, double* pos, double* vel, double* mass, double* charge, int64_t* ids) {
+int nbody_get_state(nbody_ctx* c, int order, double* pos, double* vel, double* mass, double* charge, int64_t* ids,
+                    double* acc) {
     if (!c) return NBODY_ERR_INVALID;
     if (c->n == 0) return nb_fail(c, NBODY_ERR_STATE, "no particles");
     NB_TRY(fetch(c, order ? 1 : 0));
@@ -338,6 +345,7 @@ int nbody_get_state(nbody_ctx* c, int order, double* pos, double* vel, double* m
     if (mass) NB_CU(c, cudaMemcpyAsync(mass, st + 6 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st));
     if (charge) NB_CU(c, cudaMemcpyAsync(charge, st + 7 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st));
     if (ids) NB_CU(c, cudaMemcpyAsync(ids, st + 8 * n, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, c->st));
+    if (acc) NB_CU(c, cudaMemcpyAsync(acc, st + 9 * n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->st));
     NB_CU(c, cudaStreamSynchronize(c->st));
     return NBODY_OK;
 }
@@ -389,6 +397,14 @@ int nbody_diagnostics(nbody_ctx* c, double* out) {
     NB_TRY(evaluate(c, 0, NB_INTEG_NONE, true));
     c->have_acc = c->prm.integrator == NBODY_INTEG_LEAPFROG;
     return c->rsz == 4 ? diag_t<float>(c, out) : diag_t<double>(c, out);
+}
+
+int nbody_get_stats(nbody_ctx* c, int64_t* out, int n) {
+    if (!c || !out) return NBODY_ERR_INVALID;
+    const int64_t v[7] = {(int64_t)c->h_stats[0], (int64_t)c->h_stats[1], (int64_t)c->h_stats[2], c->nnodes,
+                          c->nleaves, c->depth, c->launches};
+    for (int i = 0; i < n && i < 7; ++i) out[i] = v[i];
+    return NBODY_OK;
 }
 
 int nbody_tree_info(nbody_ctx* c, int64_t* n, int64_t* nnodes, int64_t* nleaves, int* depth) {

@@ -260,6 +260,7 @@ struct TravArgs {
     uint32_t pend_cap, p2p_cap;
     uint32_t *m2l_off, *m2l_cnt, *m2l_list;   // null unless the far-field lists are recorded
     uint32_t m2l_cap;
+    unsigned long long* stats;                // [0] M2L pairs, [1] P2P particle pairs, [2] P2P leaf pairs
     int32_t* info;
     double theta2x4;        // 4 theta^2
     double eps2;
@@ -317,7 +318,8 @@ __global__ void __launch_bounds__(32 * Prec<MODE>::trav_warps, 1) k_traverse(Tra
         for (int a = 0; a < T; ++a) Lreg[a] = S(0);
     }
 
-    uint32_t out_base = 0, n_out = 0, m_base = 0, m_pos = 0;
+    uint32_t out_base = 0, n_out = 0, m_base = 0, m_pos = 0, n_apx = 0;
+    unsigned long long src_particles = 0;     // per lane: particles of near-field partners (write pass)
     bool can_write = false, m_write = false;
     int bn = 0;
     uint32_t* out_list = tleaf ? A.p2p_list : A.pend_list;
@@ -357,6 +359,7 @@ __global__ void __launch_bounds__(32 * Prec<MODE>::trav_warps, 1) k_traverse(Tra
             if (out && pass == 1 && can_write) {
                 uint32_t pos = wpos + __popc(mo & lanemask_lt());
                 if (pos < n_out) out_list[out_base + pos] = s;
+                if (tleaf) src_particles += sn.count;
             }
             wpos += __popc(mo);
             const uint32_t md = __ballot_sync(0xffffffffu, desc);
@@ -372,6 +375,7 @@ __global__ void __launch_bounds__(32 * Prec<MODE>::trav_warps, 1) k_traverse(Tra
                 m_pos += __popc(ma);
             }
             if (pass == 1) {
+                n_apx += __popc(ma);
                 if (approx) batch[bn + __popc(ma & lanemask_lt())] = s;
                 bn += __popc(ma);
                 __syncwarp();
@@ -464,6 +468,15 @@ __global__ void __launch_bounds__(32 * Prec<MODE>::trav_warps, 1) k_traverse(Tra
     __syncwarp();
     if (bn > 0) m2l_batch(bn);
     __syncwarp();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) src_particles += __shfl_xor_sync(0xffffffffu, src_particles, o);
+    if (lane == 0) {
+        atomicAdd(&A.stats[0], (unsigned long long)n_apx);
+        if (tleaf) {
+            atomicAdd(&A.stats[1], src_particles * nt.count);
+            atomicAdd(&A.stats[2], (unsigned long long)n_out);
+        }
+    }
 
     // reduce the per-lane partial local expansions (fixed butterfly order)
 #pragma unroll
@@ -499,7 +512,16 @@ __global__ void __launch_bounds__(32 * Prec<MODE>::trav_warps, 1) k_traverse(Tra
 }
 
 // ---------------------------------------------------------------------------
-// near field + L2P + integrator epilogue: warp per leaf
+// near field + L2P + integrator epilogue
+//
+// Work item = (leaf, chunk of at most P2P_CHUNK partner leaves); a leaf with a
+// long partner list (a large sparse leaf next to a dense region) is spread
+// over several warps whose partial sums are added in chunk order by
+// k_p2p_final.  Within a warp, lanes hold target particles (groups of CT
+// lanes); NG = 32/CT groups take partner leaves round-robin.  Partner node
+// records are fetched 32 at a time (one per lane) and broadcast by shuffle;
+// each source tile is prefetched into registers while the previous one is
+// evaluated out of shared memory.
 // ---------------------------------------------------------------------------
 struct P2PArgs {
     const uint32_t* leaves;
@@ -509,6 +531,10 @@ struct P2PArgs {
     const void* src;        // S4*
     const void* L;          // H*
     const uint32_t *p2p_off, *p2p_cnt, *p2p_list;
+    const uint32_t* work_off;   // nleaves + 1: first work item of each leaf
+    int64_t nwork;
+    const uint32_t* part_off;   // nleaves + 1: partial-sum slot of each multi-chunk leaf
+    void* part;                 // R[4] per (chunk, target particle)
     void *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az;   // R*
     const void *m, *q;      // R*
     void* pot;              // R* or null
@@ -525,7 +551,52 @@ __device__ __forceinline__ void kahan_add(S& sum, S& comp, S v) {
 }
 
 constexpr int P2P_WARPS = 4;
-constexpr int P2P_TILE = 32;
+constexpr int P2P_TILE = 32;      // source particles per tile and group
+constexpr int P2P_CHUNK = 256;    // partner leaves per work item
+
+static __global__ void k_p2p_plan(int64_t nleaves, const uint32_t* __restrict__ leaves, const NodeRec* __restrict__ nodes,
+                           const uint32_t* __restrict__ p2p_cnt, uint32_t* __restrict__ nch,
+                           uint32_t* __restrict__ psize) {
+    const int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li > nleaves) return;
+    if (li == nleaves) { nch[li] = 0; psize[li] = 0; return; }
+    const uint32_t k = leaves[li];
+    const uint32_t c = (p2p_cnt[k] + P2P_CHUNK - 1) / P2P_CHUNK;
+    const uint32_t n = c > 1 ? c : 1u;
+    nch[li] = n;
+    psize[li] = n > 1 ? n * nodes[k].count : 0u;
+}
+
+template <int MODE, int P>
+__device__ __forceinline__ void p2p_epilogue(const P2PArgs& A, uint32_t i, const typename Prec<MODE>::S* sL,
+                                             typename Prec<MODE>::S4 yi, typename Prec<MODE>::R Ex,
+                                             typename Prec<MODE>::R Ey, typename Prec<MODE>::R Ez,
+                                             typename Prec<MODE>::R Ps, bool pot) {
+    typedef typename Prec<MODE>::R R;
+    typedef typename Prec<MODE>::S S;
+    S fx, fy, fz, fp;
+    Ops<S, P>::l2p(sL, yi.x, yi.y, yi.z, fx, fy, fz, fp);
+    Ex += (R)fx; Ey += (R)fy; Ez += (R)fz;
+    Ps += (R)fp;
+    const R* mq = (const R*)A.m;
+    const R* qq = (const R*)A.q;
+    const R f = (R)A.G * qq[i] / mq[i];
+    const R axv = f * Ex, ayv = f * Ey, azv = f * Ez;
+    R* X = (R*)A.x; R* Y = (R*)A.y; R* Z = (R*)A.z;
+    R* VX = (R*)A.vx; R* VY = (R*)A.vy; R* VZ = (R*)A.vz;
+    R* AX = (R*)A.ax; R* AY = (R*)A.ay; R* AZ = (R*)A.az;
+    AX[i] = axv; AY[i] = ayv; AZ[i] = azv;
+    if (A.integ == NB_INTEG_KDK_CLOSE) {
+        const R h = (R)(0.5 * A.dt);
+        VX[i] += h * axv; VY[i] += h * ayv; VZ[i] += h * azv;
+    } else if (A.integ == NB_INTEG_EULER) {
+        const R dt = (R)A.dt;
+        const R vx0 = VX[i], vy0 = VY[i], vz0 = VZ[i];
+        VX[i] = vx0 + axv * dt; VY[i] = vy0 + ayv * dt; VZ[i] = vz0 + azv * dt;
+        X[i] += vx0 * dt; Y[i] += vy0 * dt; Z[i] += vz0 * dt;
+    }
+    if (pot) ((R*)A.pot)[i] = -(R)A.G * Ps;
+}
 
 template <int MODE, int P, bool POT>
 __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p(P2PArgs A) {
@@ -539,18 +610,33 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p(P2PArgs A) {
     __shared__ S sL[P2P_WARPS][T];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
     const int64_t w = (int64_t)blockIdx.x * P2P_WARPS + wib;
-    if (w >= A.nleaves) return;
-    const uint32_t k = A.leaves[w];
+    if (w >= A.nwork) return;
+    // which leaf / chunk: last li with work_off[li] <= w
+    int64_t lo = 0, hi = A.nleaves;
+    while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (A.work_off[mid] <= (uint32_t)w) lo = mid; else hi = mid;
+    }
+    const int64_t li = lo;
+    const uint32_t chunk = (uint32_t)w - A.work_off[li];
+    const uint32_t nchunk = A.work_off[li + 1] - A.work_off[li];
+    const uint32_t k = A.leaves[li];
     const NodeRec nt = A.nodes[k];
     const double unit = A.box->unit;
     const S4* src = (const S4*)A.src;
-    const H* Lg = (const H*)A.L;
-    for (int a = lane; a < T; a += 32) sL[wib][a] = (S)Lg[(int64_t)k * T + a];
+    if (nchunk == 1) {
+        const H* Lg = (const H*)A.L;
+        for (int a = lane; a < T; a += 32) sL[wib][a] = (S)Lg[(int64_t)k * T + a];
+    }
     const uint32_t cnt_t = nt.count;
-    const int CT = cnt_t <= 4 ? 4 : cnt_t <= 8 ? 8 : cnt_t <= 16 ? 16 : 32;
-    const int NG = 32 / CT, grp = lane / CT, gl = lane % CT;
+    // lanes per target group (8, 16 or 32); NG = 32 / CT <= 4 source groups, one tile each
+    const int CT = cnt_t <= 8 ? 8 : cnt_t <= 16 ? 16 : 32;
+    const int NG = 32 / CT, grp = lane / CT, gl = lane % CT, TPL = P2P_TILE / CT;
     const uint32_t loff = A.p2p_off[k], lcnt = A.p2p_cnt[k];
+    const uint32_t s_lo = chunk * P2P_CHUNK, s_hi = min(lcnt, s_lo + P2P_CHUNK);
     const S eps2 = (S)A.eps2;
+    S4 zero4;
+    zero4.x = 0; zero4.y = 0; zero4.z = 0; zero4.w = 0;
     __syncwarp();
     for (uint32_t tc = 0; tc < cnt_t; tc += CT) {
         const uint32_t ti = tc + gl;
@@ -558,46 +644,74 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p(P2PArgs A) {
         const uint32_t i = nt.begin + (tvalid ? ti : 0);
         const S4 yi = src[i];
         S ex = 0, ey = 0, ez = 0, ps = 0, cx = 0, cy = 0, cz = 0, cp = 0;
-        const uint32_t rounds = (lcnt + NG - 1) / NG;
-        for (uint32_t rr = 0; rr < rounds; ++rr) {
-            const uint32_t li = rr * NG + grp;
-            const bool has = li < lcnt;
-            uint32_t s = 0, scount = 0, sbeg = 0;
-            S dx = 0, dy = 0, dz = 0;
-            if (has) {
-                s = A.p2p_list[loff + li];
-                const NodeRec sn = A.nodes[s];
-                scount = sn.count;
-                sbeg = sn.begin;
+        for (uint32_t base = s_lo; base < s_hi; base += 32) {
+            const uint32_t nb = min(32u, s_hi - base);
+            // partner records, one per lane
+            uint32_t my_s = 0, my_beg = 0, my_cnt = 0;
+            S my_dx = 0, my_dy = 0, my_dz = 0;
+            if ((uint32_t)lane < nb) {
+                my_s = A.p2p_list[loff + base + lane];
+                const NodeRec sn = A.nodes[my_s];
+                my_beg = sn.begin;
+                my_cnt = sn.count;
                 double ddx, ddy, ddz;
                 disp(sn, nt, unit, ddx, ddy, ddz);
-                dx = (S)ddx; dy = (S)ddy; dz = (S)ddz;
+                my_dx = (S)ddx; my_dy = (S)ddy; my_dz = (S)ddz;
             }
-            uint32_t mx = scount;
+            const uint32_t rounds = (nb + NG - 1) / NG;
+            // the sequence of steps: (round rr, sub-tile sb); fetch the first
+            uint32_t rr = 0, sb = 0;
+            const uint32_t cur_beg = __shfl_sync(0xffffffffu, my_beg, grp);
+            const uint32_t cur_cnt0 = __shfl_sync(0xffffffffu, my_cnt, grp);
+            const uint32_t cur_cnt = (uint32_t)grp < nb ? cur_cnt0 : 0u;
+            S4 pre[4];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            for (uint32_t sb = 0; sb < mx; sb += P2P_TILE) {
-                for (int e = gl; e < P2P_TILE; e += CT) {
-                    const uint32_t j = sb + e;
-                    S4 v;
-                    if (j < scount) {
-                        v = src[sbeg + j];
-                        v.x += dx; v.y += dy; v.z += dz;
-                    } else {
-                        v.x = 0; v.y = 0; v.z = 0; v.w = 0;
-                    }
-                    tile[wib][grp][e] = v;
-                }
+            for (int e = 0; e < 4; ++e) {
+                const uint32_t j = sb + gl + e * CT;
+                pre[e] = (e < TPL && j < cur_cnt) ? src[cur_beg + j] : zero4;
+            }
+            while (rr < rounds) {
+                // current step's geometry
+                const uint32_t q = rr * NG + grp;
+                const uint32_t qs = q & 31;
+                const uint32_t s_id = __shfl_sync(0xffffffffu, my_s, qs);
+                const S dx = __shfl_sync(0xffffffffu, my_dx, qs), dy = __shfl_sync(0xffffffffu, my_dy, qs),
+                        dz = __shfl_sync(0xffffffffu, my_dz, qs);
+                const uint32_t scnt0 = __shfl_sync(0xffffffffu, my_cnt, qs);
+                const uint32_t scnt = q < nb ? scnt0 : 0u;
+                uint32_t mx = scnt;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                // store the prefetched tile
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (e < TPL) tile[wib][grp][gl + e * CT] = pre[e];
                 __syncwarp();
-                const int nj = scount > sb ? min((int)(scount - sb), P2P_TILE) : 0;
+                // next step and its prefetch
+                uint32_t nrr = rr, nsb = sb + P2P_TILE;
+                if (nsb >= mx) { nrr = rr + 1; nsb = 0; }
+                {
+                    const uint32_t nq = nrr * NG + grp;
+                    const uint32_t nbeg = __shfl_sync(0xffffffffu, my_beg, nq & 31);
+                    const uint32_t ncnt0 = __shfl_sync(0xffffffffu, my_cnt, nq & 31);
+                    const uint32_t ncnt = (nrr < rounds && nq < nb) ? ncnt0 : 0u;
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const uint32_t j = nsb + gl + e * CT;
+                        pre[e] = (e < TPL && j < ncnt) ? src[nbeg + j] : zero4;
+                    }
+                }
+                // evaluate the current tile against this lane's target, shifted into the source leaf's frame
+                const S yx = yi.x - dx, yy = yi.y - dy, yz = yi.z - dz;
+                const int nj = scnt > sb ? min((int)(scnt - sb), P2P_TILE) : 0;
                 S px = 0, py = 0, pz = 0, pp = 0;
 #pragma unroll 4
                 for (int e = 0; e < nj; ++e) {
                     const S4 sj = tile[wib][grp][e];
-                    const S rx = sj.x - yi.x, ry = sj.y - yi.y, rz = sj.z - yi.z;
+                    const S rx = sj.x - yx, ry = sj.y - yy, rz = sj.z - yz;
                     const S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
                     S inv = s2 > S(0) ? nb_rsqrt(s2) : S(0);
-                    if (POT && s == k && sb + e == ti) inv = S(0);
+                    if (POT && s_id == k && sb + e == ti) inv = S(0);
                     const S w3 = sj.w * inv * inv * inv;
                     px = nb_fma(rx, w3, px);
                     py = nb_fma(ry, w3, py);
@@ -612,6 +726,8 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p(P2PArgs A) {
                     if (POT) ps += pp;
                 }
                 __syncwarp();
+                rr = nrr;
+                sb = nsb;
             }
         }
         // combine the source groups in a fixed order, in the state precision
@@ -621,30 +737,45 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p(P2PArgs A) {
             if (POT) Ps += shfl_xor_t(Ps, o);
         }
         if (grp == 0 && tvalid) {
-            S fx, fy, fz, fp;
-            Ops<S, P>::l2p(sL[wib], yi.x, yi.y, yi.z, fx, fy, fz, fp);
-            Ex += (R)fx; Ey += (R)fy; Ez += (R)fz;
-            if (POT) Ps += (R)fp;
-            const R* mq = (const R*)A.m;
-            const R* qq = (const R*)A.q;
-            const R f = (R)A.G * qq[i] / mq[i];
-            const R axv = f * Ex, ayv = f * Ey, azv = f * Ez;
-            R* X = (R*)A.x; R* Y = (R*)A.y; R* Z = (R*)A.z;
-            R* VX = (R*)A.vx; R* VY = (R*)A.vy; R* VZ = (R*)A.vz;
-            R* AX = (R*)A.ax; R* AY = (R*)A.ay; R* AZ = (R*)A.az;
-            AX[i] = axv; AY[i] = ayv; AZ[i] = azv;
-            if (A.integ == NB_INTEG_KDK_CLOSE) {
-                const R h = (R)(0.5 * A.dt);
-                VX[i] += h * axv; VY[i] += h * ayv; VZ[i] += h * azv;
-            } else if (A.integ == NB_INTEG_EULER) {
-                const R dt = (R)A.dt;
-                const R vx0 = VX[i], vy0 = VY[i], vz0 = VZ[i];
-                VX[i] = vx0 + axv * dt; VY[i] = vy0 + ayv * dt; VZ[i] = vz0 + azv * dt;
-                X[i] += vx0 * dt; Y[i] += vy0 * dt; Z[i] += vz0 * dt;
+            if (nchunk == 1) {
+                p2p_epilogue<MODE, P>(A, i, sL[wib], yi, Ex, Ey, Ez, Ps, POT);
+            } else {
+                R* pt = (R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)chunk * cnt_t + ti);
+                pt[0] = Ex; pt[1] = Ey; pt[2] = Ez; pt[3] = Ps;
             }
-            if (POT) ((R*)A.pot)[i] = -(R)A.G * Ps;
         }
         __syncwarp();
+    }
+}
+
+// sums the chunk partials of multi-chunk leaves in chunk order, then L2P + epilogue
+template <int MODE, int P, bool POT>
+__global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p_final(P2PArgs A) {
+    typedef typename Prec<MODE>::R R;
+    typedef typename Prec<MODE>::S S;
+    typedef typename Prec<MODE>::H H;
+    typedef typename Prec<MODE>::S4 S4;
+    constexpr int T = nb_terms<P>::value;
+    __shared__ S sL[P2P_WARPS][T];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int64_t li = (int64_t)blockIdx.x * P2P_WARPS + wib;
+    if (li >= A.nleaves) return;
+    const uint32_t nchunk = A.work_off[li + 1] - A.work_off[li];
+    if (nchunk <= 1) return;
+    const uint32_t k = A.leaves[li];
+    const NodeRec nt = A.nodes[k];
+    const H* Lg = (const H*)A.L;
+    for (int a = lane; a < T; a += 32) sL[wib][a] = (S)Lg[(int64_t)k * T + a];
+    __syncwarp();
+    const S4* src = (const S4*)A.src;
+    for (uint32_t ti = lane; ti < nt.count; ti += 32) {
+        R e[4] = {0, 0, 0, 0};
+        for (uint32_t c = 0; c < nchunk; ++c) {
+            const R* pt = (const R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)c * nt.count + ti);
+            e[0] += pt[0]; e[1] += pt[1]; e[2] += pt[2]; e[3] += pt[3];
+        }
+        const uint32_t i = nt.begin + ti;
+        p2p_epilogue<MODE, P>(A, i, sL[wib], src[i], e[0], e[1], e[2], e[3], POT);
     }
 }
 
@@ -676,12 +807,14 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
         c->nleaves, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes), box, DP<R>(c->x[cur]), DP<R>(c->y[cur]),
         DP<R>(c->z[cur]), DP<R>(c->q[cur]), DP<S4>(c->src), DP<H>(c->M), M32);
     NB_LAUNCHED(c, "p2m");
+    c->launches += 1;
     for (int l = c->depth - 1; l >= 0; --l) {
         const int lo = c->level_start[l], hi = c->level_start[l + 1];
         if (hi <= lo) continue;
         k_m2m<MODE, P><<<(unsigned)((hi - lo + 3) / 4), 128, 0, c->st>>>(lo, hi, DP<NodeRec>(c->nodes), box,
                                                                          DP<H>(c->M), M32);
         NB_LAUNCHED(c, "m2m");
+        c->launches += 1;
     }
     if (c->timing) cudaEventRecord(c->ev[4], c->st);
 
@@ -702,6 +835,8 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
             NB_CU(c, cudaMemsetAsync(c->m2l_cnt.p, 0, sizeof(uint32_t) * nn, c->st));
         }
         int32_t* info = DP<int32_t>(c->info);
+        NB_TRY(nb_grow(c, c->stats, 8 * sizeof(unsigned long long)));
+        NB_CU(c, cudaMemsetAsync(c->stats.p, 0, 8 * sizeof(unsigned long long), c->st));
         NB_CU(c, cudaMemsetAsync(info + INFO_PEND_TAIL, 0, 3 * sizeof(int32_t), c->st));
         NB_CU(c, cudaMemsetAsync(info + INFO_ERR, 0, sizeof(int32_t), c->st));
         k_root<MODE, P><<<1, 32, 0, c->st>>>(DP<NodeRec>(c->nodes), DP<H>(c->L), DP<uint32_t>(c->pend_off),
@@ -709,6 +844,7 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
                                              DP<uint32_t>(c->p2p_off), DP<uint32_t>(c->p2p_cnt),
                                              DP<uint32_t>(c->p2p_list), info);
         NB_LAUNCHED(c, "root");
+        c->launches += 1;
         TravArgs A;
         A.nodes = DP<NodeRec>(c->nodes);
         A.box = box;
@@ -723,6 +859,7 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
         A.m2l_off = c->record_m2l ? DP<uint32_t>(c->m2l_off) : nullptr;
         A.m2l_cnt = c->record_m2l ? DP<uint32_t>(c->m2l_cnt) : nullptr;
         A.m2l_cap = (uint32_t)c->m2l_cap;
+        A.stats = DP<unsigned long long>(c->stats);
         A.info = info;
         const float th = (float)c->prm.theta;
         A.theta2x4 = 4.0 * (double)(th * th);
@@ -734,8 +871,28 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
             const int W = Prec<MODE>::trav_warps;
             k_traverse<MODE, P><<<(unsigned)((A.hi - A.lo + W - 1) / W), 32 * W, smem, c->st>>>(A);
             NB_LAUNCHED(c, "traverse");
+            c->launches += 1;
+        }
+        // near-field work plan: chunks per leaf and partial-sum slots, scanned
+        {
+            const int64_t nl = c->nleaves;
+            NB_TRY(nb_grow(c, c->p2p_nch, sizeof(uint32_t) * (nl + 1)));
+            NB_TRY(nb_grow(c, c->p2p_work_off, sizeof(uint32_t) * (nl + 1)));
+            NB_TRY(nb_grow(c, c->p2p_psize, sizeof(uint32_t) * (nl + 1)));
+            NB_TRY(nb_grow(c, c->p2p_part_off, sizeof(uint32_t) * (nl + 1)));
+            k_p2p_plan<<<(unsigned)((nl + 1 + 255) / 256), 256, 0, c->st>>>(
+                nl, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes), DP<uint32_t>(c->p2p_cnt), DP<uint32_t>(c->p2p_nch),
+                DP<uint32_t>(c->p2p_psize));
+            NB_LAUNCHED(c, "p2p_plan");
+            c->launches += 1;
+            NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->p2p_nch), DP<uint32_t>(c->p2p_work_off), nl + 1,
+                               (uint32_t*)(info + INFO_P2P_WORK)));
+            NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->p2p_psize), DP<uint32_t>(c->p2p_part_off), nl + 1,
+                               (uint32_t*)(info + INFO_P2P_PART)));
         }
         NB_CU(c, cudaMemcpyAsync(c->h_info, info, sizeof(int32_t) * INFO_WORDS, cudaMemcpyDeviceToHost, c->st));
+        NB_CU(c, cudaMemcpyAsync(c->h_stats, c->stats.p, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 c->st));
         NB_CU(c, cudaStreamSynchronize(c->st));
         const uint32_t e = (uint32_t)c->h_info[INFO_ERR];
         if (e & NB_ERRBIT_STACK) return nb_fail(c, NBODY_ERR_CAPACITY, "traversal descent stack overflow");
@@ -750,6 +907,10 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     }
     if (c->timing) cudaEventRecord(c->ev[5], c->st);
 
+    const int64_t nl = c->nleaves;
+    const int64_t nwork = (uint32_t)c->h_info[INFO_P2P_WORK];
+    const int64_t npart = (uint32_t)c->h_info[INFO_P2P_PART];
+    NB_TRY(nb_grow(c, c->p2p_part, sizeof(R) * 4 * (size_t)(npart + 1)));
     P2PArgs B;
     B.leaves = DP<uint32_t>(c->leaves);
     B.nleaves = c->nleaves;
@@ -758,6 +919,10 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     B.src = c->src.p;
     B.L = c->L.p;
     B.p2p_off = DP<uint32_t>(c->p2p_off); B.p2p_cnt = DP<uint32_t>(c->p2p_cnt); B.p2p_list = DP<uint32_t>(c->p2p_list);
+    B.work_off = DP<uint32_t>(c->p2p_work_off);
+    B.nwork = nwork;
+    B.part_off = DP<uint32_t>(c->p2p_part_off);
+    B.part = c->p2p_part.p;
     B.x = c->x[cur].p; B.y = c->y[cur].p; B.z = c->z[cur].p;
     B.vx = c->vx[cur].p; B.vy = c->vy[cur].p; B.vz = c->vz[cur].p;
     B.ax = c->ax[cur].p; B.ay = c->ay[cur].p; B.az = c->az[cur].p;
@@ -767,10 +932,17 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     B.G = c->prm.G;
     B.dt = c->prm.dt;
     B.integ = integ;
-    const unsigned g = (unsigned)((c->nleaves + P2P_WARPS - 1) / P2P_WARPS);
-    if (want_pot) k_p2p<MODE, P, true><<<g, 32 * P2P_WARPS, 0, c->st>>>(B);
-    else k_p2p<MODE, P, false><<<g, 32 * P2P_WARPS, 0, c->st>>>(B);
+    const unsigned g = (unsigned)((nwork + P2P_WARPS - 1) / P2P_WARPS);
+    const unsigned gf = (unsigned)((nl + P2P_WARPS - 1) / P2P_WARPS);
+    if (want_pot) {
+        k_p2p<MODE, P, true><<<g, 32 * P2P_WARPS, 0, c->st>>>(B);
+        if (npart) k_p2p_final<MODE, P, true><<<gf, 32 * P2P_WARPS, 0, c->st>>>(B);
+    } else {
+        k_p2p<MODE, P, false><<<g, 32 * P2P_WARPS, 0, c->st>>>(B);
+        if (npart) k_p2p_final<MODE, P, false><<<gf, 32 * P2P_WARPS, 0, c->st>>>(B);
+    }
     NB_LAUNCHED(c, "p2p");
+    c->launches += npart ? 2 : 1;
     if (c->timing) cudaEventRecord(c->ev[6], c->st);
     return NBODY_OK;
 }

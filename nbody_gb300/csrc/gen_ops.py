@@ -82,6 +82,34 @@ def gen_derivs(p, o):
     o.append("  }")
 
 
+def m2l_flops(p):
+    """Flops of one far-field cell pair at order p: displacement (3), s (5),
+    reciprocal and rsqrt (2), each derivative entry (its products, sums and
+    the scaling), and the contraction (one FMA = 2 per (n, k) pair)."""
+    f = 3 + 5 + 2
+    for n in terms(p)[1:]:
+        i = 0 if n[0] > 0 else (1 if n[1] > 0 else 2)
+        k = 0
+        f2 = 0
+        c = 2 * n[i] - 1
+        f2 += 2 if c != 1 else 1
+        k += 1
+        for d in range(3):
+            if d != i and n[d] >= 1:
+                f2 += 2
+                k += 1
+        if n[i] >= 2:
+            f2 += 1 if (n[i] - 1) ** 2 != 1 else 0
+            k += 1
+        for d in range(3):
+            if d != i and n[d] >= 2:
+                f2 += 1
+                k += 1
+        f += f2 + (k - 1) + 1
+    pairs = sum(T(p - sum(n)) for n in terms(p))
+    return f + 2 * pairs
+
+
 def gen_m2l(p, o):
     # L[k] += sum_n (-1)^|n| M[n] D[n+k]; M streamed from memory
     o.append("  template <int ST = 1>")
@@ -187,6 +215,8 @@ def main():
              ",".join(f"{{{a},{b},{c}}}" for a, b, c in ts) + "};")
     o.append(f"__device__ const double nb_invfact[{T(PMAX)}] = {{" +
              ",".join(repr(1.0 / (fact[a] * fact[b] * fact[c])) for a, b, c in ts) + "};")
+    o.append("constexpr long long nb_m2l_flops_tab[" + str(PMAX + 1) + "] = {0," +
+             ",".join(str(m2l_flops(p)) for p in range(1, PMAX + 1)) + "};")
     o.append("template <int P> struct Tabs;")
     for p in range(1, PMAX + 1):
         o.append(f"template <> struct Tabs<{p}> {{")

@@ -32,6 +32,8 @@ enum {
     INFO_P2P_TAIL = 5,
     INFO_M2L_TAIL = 6,
     INFO_HIST = 8,                 // 8 .. 8+NB_LEVELS: nodes per level
+    INFO_P2P_WORK = 30,            // near-field work items
+    INFO_P2P_PART = 31,            // near-field partial-sum slots
     INFO_WORDS = 32
 };
 
@@ -89,6 +91,10 @@ struct nbody_ctx {
     size_t m2l_cap = 0;
     DevBuf stage;                  // host <-> device staging (interleaved doubles)
     DevBuf diag;
+    DevBuf stats;                  // 8 x uint64 work counters of the last evaluation
+    DevBuf p2p_nch, p2p_work_off, p2p_psize, p2p_part_off, p2p_part;   // near-field work plan
+    unsigned long long h_stats[8] = {0};
+    int64_t launches = 0;          // kernels launched by the last force evaluation
 
     // small device blocks + pinned mirrors
     DevBuf info, box, bbox;

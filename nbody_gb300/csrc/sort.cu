@@ -151,6 +151,7 @@ int nb_scan_u32(nbody_ctx* c, const uint32_t* in, uint32_t* out, int64_t n, uint
     k_scan_partials<<<1, 1024, 0, c->st>>>(part, nb, total_dev);
     k_scan_down<<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(in, out, n, part);
     NB_LAUNCHED(c, "scan");
+    c->launches += 3;
     return NBODY_OK;
 }
 
@@ -173,6 +174,7 @@ int nb_radix_sort(nbody_ctx* c, int64_t n, uint64_t* k0, uint32_t* v0, uint64_t*
         k_radix_scatter<<<nblocks, RADIX_THREADS, 0, c->st>>>(ki, vi, ko, vo, n, sh, mask, DP<uint32_t>(c->hist_scan),
                                                                nblocks);
         NB_LAUNCHED(c, "radix_scatter");
+        c->launches += 2;
         uint64_t* tk = ki; ki = ko; ko = tk;
         uint32_t* tv = vi; vi = vo; vo = tv;
         *result_in_first = !*result_in_first;

@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(TB) k_kick_drift_bbox(int64_t n, StatePtrs<R> 
             atomicMax(&bbox[3 + d], ord_key(mx[d]));
         }
     }
-    if (bad) atomicOr((unsigned int*)&info[INFO_ERR], 16u);
+    if (bad) atomicOr((unsigned int*)&info[INFO_ERR], NB_ERRBIT_NONFINITE);
 }
 
 // root box: fixed (the reference's [0, bounds)) or the power-of-two data cube
@@ -289,6 +289,7 @@ template <typename R>
 int begin_step_t(nbody_ctx* c, int kdk) {
     const int64_t n = c->n;
     unsigned long long* bb = DP<unsigned long long>(c->bbox);
+    NB_CU(c, cudaMemsetAsync(c->info.p, 0, sizeof(int32_t), c->st));   // INFO_ERR
     NB_CU(c, cudaMemsetAsync(bb, 0xff, 3 * sizeof(unsigned long long), c->st));
     NB_CU(c, cudaMemsetAsync(bb + 3, 0x00, 3 * sizeof(unsigned long long), c->st));
     unsigned g = nblk(n);
@@ -301,6 +302,7 @@ int begin_step_t(nbody_ctx* c, int kdk) {
     k_keys<R><<<nblk(n), TB, 0, c->st>>>(n, DP<R>(c->x[c->cur]), DP<R>(c->y[c->cur]), DP<R>(c->z[c->cur]),
                                          DP<BoxDev>(c->box), DP<uint64_t>(c->keys[0]), DP<uint32_t>(c->vals[0]));
     NB_LAUNCHED(c, "kick_drift_keys");
+    c->launches += 3;
     return NBODY_OK;
 }
 
@@ -309,6 +311,7 @@ int gather_t(nbody_ctx* c) {
     k_gather<R><<<nblk(c->n), TB, 0, c->st>>>(c->n, DP<uint32_t>(c->vals[0]), state<R>(c, c->cur),
                                               state<R>(c, 1 - c->cur));
     NB_LAUNCHED(c, "gather");
+    c->launches += 1;
     c->cur = 1 - c->cur;
     return NBODY_OK;
 }
@@ -339,9 +342,12 @@ int nb_build_tree(nbody_ctx* c) {
     k_tree_chain<<<nblk(n), TB, 0, c->st>>>(n, C, c->prm.max_level, DP<int32_t>(c->cpl), DP<int32_t>(c->wnd),
                                             DP<uint32_t>(c->nc), info);
     NB_LAUNCHED(c, "tree_chain");
+    c->launches += 2;
     NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->nc), DP<uint32_t>(c->pfx), n, (uint32_t*)(info + INFO_NNODES)));
     NB_CU(c, cudaMemcpyAsync(c->h_info, info, sizeof(int32_t) * INFO_WORDS, cudaMemcpyDeviceToHost, c->st));
     NB_CU(c, cudaStreamSynchronize(c->st));
+    if ((uint32_t)c->h_info[INFO_ERR] & NB_ERRBIT_NONFINITE)
+        return nb_fail(c, NBODY_ERR_STATE, "non-finite particle position");
     c->nnodes = (uint32_t)c->h_info[INFO_NNODES];
     c->nleaves = c->h_info[INFO_NLEAVES];
     c->depth = c->h_info[INFO_DEPTH];
@@ -364,6 +370,7 @@ int nb_build_tree(nbody_ctx* c) {
     k_tree_seeds<<<nblk(n), TB, 0, c->st>>>(n, DP<int32_t>(c->cpl), DP<uint32_t>(c->nc), DP<uint32_t>(c->pfx),
                                             DP<uint64_t>(c->seedk[0]), DP<uint32_t>(c->seedv[0]));
     NB_LAUNCHED(c, "tree_seeds");
+    c->launches += 1;
     int first = 1;
     NB_TRY(nb_radix_sort(c, nn, DP<uint64_t>(c->seedk[0]), DP<uint32_t>(c->seedv[0]), DP<uint64_t>(c->seedk[1]),
                          DP<uint32_t>(c->seedv[1]), 0, 8, &first));
@@ -374,9 +381,11 @@ int nb_build_tree(nbody_ctx* c) {
                                              DP<uint32_t>(c->seedv[si]), ls, DP<NodeRec>(c->nodes),
                                              DP<uint32_t>(c->leafflag));
     NB_LAUNCHED(c, "tree_nodes");
+    c->launches += 1;
     NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->leafflag), DP<uint32_t>(c->leafpfx), nn, nullptr));
     k_tree_leaves<<<nblk(nn), TB, 0, c->st>>>(nn, DP<uint32_t>(c->leafflag), DP<uint32_t>(c->leafpfx),
                                               DP<uint32_t>(c->leaves));
     NB_LAUNCHED(c, "tree_leaves");
+    c->launches += 1;
     return NBODY_OK;
 }

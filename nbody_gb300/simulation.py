@@ -112,24 +112,26 @@ class CudaSimulation:
         self.close()
 
     # -- state --------------------------------------------------------------
-    def set_state(self, pos, vel=None, mass=None, charge=None):
+    def set_state(self, pos, vel=None, mass=None, charge=None, acc=None):
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
         n = pos.shape[0]
         vel = np.zeros((n, 3)) if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(n, 3)
         mass = np.ones(n) if mass is None else np.ascontiguousarray(mass, dtype=np.float64).reshape(n)
         charge = None if charge is None else np.ascontiguousarray(charge, dtype=np.float64).reshape(n)
-        check(self._h, _lib.load().nbody_set_state(self._h, n, ptr(pos), ptr(vel), ptr(mass), ptr(charge)))
+        acc = None if acc is None else np.ascontiguousarray(acc, dtype=np.float64).reshape(n, 3)
+        check(self._h, _lib.load().nbody_set_state(self._h, n, ptr(pos), ptr(vel), ptr(mass), ptr(charge), ptr(acc)))
         self.n = n
 
-    def state(self, order: str = "input"):
-        """(pos, vel, mass, charge, ids); order 'input' or 'leaf' (Morton)."""
+    def state(self, order: str = "input", with_acc: bool = False):
+        """(pos, vel, mass, charge, ids[, acc]); order 'input' or 'leaf' (Morton)."""
         n = self.n
         pos, vel = np.empty((n, 3)), np.empty((n, 3))
         mass, charge = np.empty(n), np.empty(n)
         ids = np.empty(n, np.int64)
+        acc = np.empty((n, 3)) if with_acc else None
         check(self._h, _lib.load().nbody_get_state(self._h, 1 if order == "input" else 0, ptr(pos), ptr(vel),
-                                                   ptr(mass), ptr(charge), ptr(ids)))
-        return pos, vel, mass, charge, ids
+                                                   ptr(mass), ptr(charge), ptr(ids), ptr(acc)))
+        return (pos, vel, mass, charge, ids, acc) if with_acc else (pos, vel, mass, charge, ids)
 
     # -- the reference interface ---------------------------------------------
     def step(self, nsteps: int = 1) -> float:
@@ -185,6 +187,20 @@ class CudaSimulation:
         out = np.empty((max(k.value, 1), 2), np.int32)
         check(self._h, L.nbody_get_interactions(self._h, w, C.byref(k), ptr(out)))
         return out[: k.value]
+
+    def direct(self, targets):
+        """FP64 softened direct-sum accelerations and potentials of the targets (input indices), on the GPU."""
+        tg = np.ascontiguousarray(targets, dtype=np.int64)
+        acc = np.empty((len(tg), 3))
+        pot = np.empty(len(tg))
+        check(self._h, _lib.load().nbody_direct_forces(self._h, len(tg), ptr(tg), ptr(acc), ptr(pot)))
+        return acc, pot
+
+    def stats(self):
+        out = np.zeros(7, np.int64)
+        check(self._h, _lib.load().nbody_get_stats(self._h, ptr(out), 7))
+        keys = ("m2l_pairs", "p2p_particle_pairs", "p2p_leaf_pairs", "nodes", "leaves", "depth", "launches")
+        return dict(zip(keys, (int(v) for v in out)))
 
     def set_timing(self, on: bool = True):
         check(self._h, _lib.load().nbody_set_timing(self._h, int(on)))

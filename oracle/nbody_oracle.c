@@ -684,6 +684,32 @@ float orc_naive_steps(int n, float* pos, float* vel, const float* mass, const fl
     return time;
 }
 
+/* The same serial loop restricted to rows i in [i0, i1) of the triangle
+   (every j < i), i.e. a bounded sample of one step of
+   src/naive_simulation.cpp:8-34 with identical per-pair arithmetic and
+   update order.  Positions are not drifted.  Returns the pairs evaluated. */
+int64_t orc_naive_rows(int n, const float* pos, float* vel, const float* mass, const float* charge, float G, float dt,
+                       int i0, int i1, int fix_delta) {
+    int64_t pairs = 0;
+    for (unsigned i = (unsigned)(i0 < 1 ? 1 : i0); i < (unsigned)i1 && i < (unsigned)n; ++i) {
+        for (unsigned j = 0; j < i; ++j) {
+            float d0 = pos[4 * j] - pos[4 * i];
+            float d1 = fix_delta ? pos[4 * j + 1] - pos[4 * i + 1] : pos[4 * j] - pos[4 * i];
+            float d2 = fix_delta ? pos[4 * j + 2] - pos[4 * i + 2] : pos[4 * j] - pos[4 * i];
+            float r = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+            float cf = charge[i] * charge[j];
+            float ma = mass[i], mb = mass[j];
+            float f0 = G * cf * d0 / (r * r * r);
+            float f1 = G * cf * d1 / (r * r * r);
+            float f2 = G * cf * d2 / (r * r * r);
+            vel[4 * i] += f0 / ma * dt; vel[4 * i + 1] += f1 / ma * dt; vel[4 * i + 2] += f2 / ma * dt;
+            vel[4 * j] -= f0 / mb * dt; vel[4 * j + 1] -= f1 / mb * dt; vel[4 * j + 2] -= f2 / mb * dt;
+        }
+        pairs += i;
+    }
+    return pairs;
+}
+
 /* Threaded form of the same per-pair arithmetic for timing on many cores:
    each thread owns a block of targets i and sums over every j != i (so each
    unordered pair is evaluated twice instead of once with Newton's third

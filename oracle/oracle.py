@@ -69,6 +69,8 @@ def lib():
     L.orc_naive_kick_mt.restype = C.c_int64
     L.orc_naive_kick_mt.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_float, C.c_int, C.c_int,
                                     C.c_int, C.c_int]
+    L.orc_naive_rows.restype = C.c_int64
+    L.orc_naive_rows.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int]
     L.orc_morton_keys.argtypes = [C.c_int64, _f64p, _f64p, _u64p]
     L.orc_derivs.argtypes = [C.c_int, _f64p, C.c_double, _f64p]
     L.orc_nterms.restype = C.c_int
