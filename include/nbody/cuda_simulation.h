@@ -1,0 +1,153 @@
+/*
+ * nbody/cuda_simulation.h -- nbody::CudaSimulation, the GB300 drop-in for
+ * nbody::OpenClSimulation (include/nbody/open_cl_simulation.h:19-203 of
+ * duanebyer/nbody).  Header-only; link with libnbody_gb300.so.
+ *
+ * Same constructor as the reference, (bounds, particles, timeStep, log), with
+ * the reference's defaults (order-1 expansion, leaf capacity 8, theta 0.5,
+ * softening 0.01, G = 1, single precision, explicit Euler, root box
+ * [0, bounds)); an overload takes an nbody_params for the other forms.
+ * step() returns the new time; particles() returns the particles in octree
+ * leaf (Morton) order like the reference's (src/open_cl_simulation.cpp:53-68).
+ * Failures throw std::runtime_error carrying the library's message, as the
+ * reference throws std::runtime_error (src/open_cl_simulation.cpp:630,648,767).
+ *
+ * A program written against the reference switches by changing its typedef:
+ *     using Simulation = nbody::CudaSimulation;
+ */
+#ifndef NBODY_CUDA_SIMULATION_H
+#define NBODY_CUDA_SIMULATION_H
+
+#include <algorithm>
+#include <initializer_list>
+#include <ostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "nbody/simulation.h"
+#include "nbody_gb300.h"
+
+namespace nbody {
+namespace cuda {
+
+/* 4-float vector indexed like the reference's device::vector_t
+   (include/nbody/device/types.h:49-74): brace-initialised, operator[]. */
+class alignas(16) vector_t final {
+    float _v[4];
+
+public:
+    vector_t() : _v{0, 0, 0, 0} {}
+    vector_t(std::initializer_list<float> list) : _v{0, 0, 0, 0} {
+        unsigned i = 0;
+        for (float x : list) {
+            if (i < 4) _v[i++] = x;
+        }
+    }
+    float& operator[](unsigned i) { return _v[i]; }
+    float const& operator[](unsigned i) const { return _v[i]; }
+};
+
+}  // namespace cuda
+
+class CudaSimulation final : public Simulation<float, cuda::vector_t> {
+    nbody_ctx* _ctx = nullptr;
+    std::ostream& _log;
+    int64_t _n = 0;
+
+    void check(int rc, const char* what) const {
+        if (rc != NBODY_OK) {
+            const char* msg = nbody_last_error(_ctx);
+            throw std::runtime_error(std::string(what) + ": " + (msg ? msg : ""));
+        }
+    }
+
+    static nbody_params defaults(Vector bounds) {
+        nbody_params p;
+        nbody_default_params(&p);
+        p.fixed_box = 1;
+        p.box_min[0] = p.box_min[1] = p.box_min[2] = 0.0;
+        p.box_size = std::max(std::max(bounds[0], bounds[1]), bounds[2]);
+        return p;
+    }
+
+    void init(nbody_params p, std::vector<Particle> const& particles, Scalar timeStep) {
+        p.dt = timeStep;
+        int rc = nbody_create(&p, &_ctx);
+        if (rc != NBODY_OK) throw std::runtime_error(std::string("nbody_create: ") + nbody_last_error(nullptr));
+        _n = (int64_t)particles.size();
+        std::vector<double> pos(3 * _n), vel(3 * _n), mass(_n), charge(_n);
+        for (int64_t i = 0; i < _n; ++i) {
+            for (int d = 0; d < 3; ++d) {
+                pos[3 * i + d] = particles[i].position[d];
+                vel[3 * i + d] = particles[i].velocity[d];
+            }
+            mass[i] = particles[i].mass;
+            charge[i] = particles[i].charge;
+        }
+        if (_n > 0)
+            check(nbody_set_state(_ctx, _n, pos.data(), vel.data(), mass.data(), charge.data(), nullptr),
+                  "nbody_set_state");
+    }
+
+    std::vector<Particle> fetch(int order) const {
+        std::vector<Particle> out;
+        if (_n == 0) return out;
+        std::vector<double> pos(3 * _n), vel(3 * _n), mass(_n), charge(_n);
+        check(nbody_get_state(_ctx, order, pos.data(), vel.data(), mass.data(), charge.data(), nullptr, nullptr),
+              "nbody_get_state");
+        out.reserve(_n);
+        for (int64_t i = 0; i < _n; ++i) {
+            Vector p = {(float)pos[3 * i], (float)pos[3 * i + 1], (float)pos[3 * i + 2], 0.0f};
+            Vector v = {(float)vel[3 * i], (float)vel[3 * i + 1], (float)vel[3 * i + 2], 0.0f};
+            out.push_back(Particle(p, v, (Scalar)mass[i], (Scalar)charge[i]));
+        }
+        return out;
+    }
+
+public:
+    CudaSimulation(Vector bounds, std::vector<Particle> particles, Scalar timeStep, std::ostream& log) : _log(log) {
+        _log << "Initializing CUDA.\n";
+        init(defaults(bounds), particles, timeStep);
+    }
+
+    CudaSimulation(Vector bounds, std::vector<Particle> particles, Scalar timeStep, std::ostream& log,
+                   nbody_params params)
+        : _log(log) {
+        if (params.fixed_box) {
+            nbody_params d = defaults(bounds);
+            params.box_size = d.box_size;
+            params.box_min[0] = params.box_min[1] = params.box_min[2] = 0.0;
+        }
+        init(params, particles, timeStep);
+    }
+
+    CudaSimulation(CudaSimulation const&) = delete;
+    CudaSimulation& operator=(CudaSimulation const&) = delete;
+
+    ~CudaSimulation() override { nbody_destroy(_ctx); }
+
+    Scalar step() override {
+        double t = 0.0;
+        check(nbody_step(_ctx, 1, &t), "nbody_step");
+        return (Scalar)t;
+    }
+
+    std::vector<Particle> particles() const override { return fetch(0); }
+
+    /* additions beyond the reference interface */
+    std::vector<Particle> particlesInInputOrder() const { return fetch(1); }
+
+    /* accelerations (n x 3, input order) at the current positions */
+    std::vector<double> computeForces() {
+        std::vector<double> acc(3 * _n);
+        check(nbody_compute_forces(_ctx, acc.data(), nullptr), "nbody_compute_forces");
+        return acc;
+    }
+
+    nbody_ctx* handle() const { return _ctx; }
+};
+
+}  // namespace nbody
+
+#endif
