@@ -112,6 +112,26 @@ int nbody_diagnostics(nbody_ctx* c, double* out);
    its CPU path src/naive_simulation.cpp is a direct sum without softening). */
 int nbody_direct_forces(nbody_ctx* c, int64_t nt, const int64_t* targets, double* acc, double* pot);
 
+/* Allocation-free form of nbody_direct_forces, for callers that must not
+   allocate device memory (code under a host framework that owns the device
+   memory budget, or on a path where cudaMalloc's synchronization or failure
+   under memory pressure is unacceptable).  No counterpart in the reference.
+   Inputs and outputs are the caller's device-accessible arrays: pos (n x 3),
+   mass and charge (n; charge may be NULL = mass), targets (nt indices into
+   them), acc (nt x 3) and pot (nt, may be NULL).  Work is enqueued on
+   `stream` (a cudaStream_t, NULL = default stream) and the call returns
+   without waiting; outputs are valid once the stream is synchronized.
+   Scratch is a fixed 4 MiB device array inside the library, so nt is limited
+   to 131072 per call (larger requests fail with NBODY_ERR_INVALID).  Every
+   call on a device shares that array: calls that overlap on the GPU race and
+   must be ordered by the caller.  The first call on a device looks up the
+   array's device address; make it before any stream capture on that device.
+   Target indices outside [0, n) give NaN results.  Errors:
+   nbody_last_error(NULL). */
+int nbody_direct_forces_static(int device, int64_t n, const double* pos, const double* mass, const double* charge,
+                               double eps, double G, int64_t nt, const int64_t* targets, double* acc, double* pot,
+                               void* stream);
+
 /* Work counters of the last force evaluation: out[0] far-field (M2L)
    cell pairs, out[1] near-field particle pairs, out[2] near-field leaf
    pairs, out[3] nodes, out[4] leaves, out[5] depth, out[6] kernel launches
