@@ -2,9 +2,10 @@
 """Throughput of the GB300 FMM step: particle-steps/s at N = 1,048,576.
 
 Workload (default): two Plummer spheres of 524,288 bodies colliding
-(eps 0.005, dt 5e-4, theta 0.5, leapfrog), mixed precision, Cartesian order 7
-(the lowest order whose rms force error vs the FP64 direct sum is <= 1e-4 on
-this workload; the error is measured and reported in every run).
+(eps 0.005, dt 5e-4, theta 0.5, leapfrog), mixed precision, Cartesian order 5,
+leaf capacity 64 (the fastest setting whose rms force error vs the FP64 direct
+sum is <= 1e-4 on this workload; the error is measured and reported in every
+run).
 
   value     device-timed particle-steps/s with the state resident in HBM
   e2e       the same through the C ABI with host buffers: every step uploads
@@ -173,8 +174,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1048576)
-    ap.add_argument("--order", type=int, default=7)
-    ap.add_argument("--cap", type=int, default=32)
+    ap.add_argument("--order", type=int, default=5)
+    ap.add_argument("--cap", type=int, default=64)
     ap.add_argument("--precision", default="mixed", choices=["fp32", "mixed", "fp64"])
     ap.add_argument("--theta", type=float, default=0.5)
     ap.add_argument("--eps", type=float, default=0.005)
@@ -218,7 +219,7 @@ def main():
 
     # timed region: K steps, state resident in HBM, per-phase CUDA events on the library's stream
     sim.set_timing(True)
-    phases = np.zeros(6)
+    phases = np.zeros(7)
     clocks = ClockSampler(local)
     torch.cuda.synchronize()
     if world > 1:
@@ -273,21 +274,22 @@ def main():
             torch.distributed.destroy_process_group()
         return 0
 
-    # roofline of the dominant kernel (per step: one near-field launch; one traversal launch per level)
+    # roofline of the dominant kernel (per step: one M2L launch, one near-field launch)
     peaks = np.zeros(2)
     L.nbody_measure_peaks(local, ptr(peaks))
     fp32_peak_tf = peaks[0] / 1e3
     per_step = phases / a.steps
     p2p_flops = stats["p2p_particle_pairs"] * L.nbody_flops_per_p2p()
     m2l_flops = stats["m2l_pairs"] * L.nbody_flops_per_m2l(a.order)
-    p2p_tf = p2p_flops / (per_step[5] * 1e-3) / 1e12 if per_step[5] > 0 else 0.0
-    trav_tf = m2l_flops / (per_step[4] * 1e-3) / 1e12 if per_step[4] > 0 else 0.0
+    p2p_tf = p2p_flops / (per_step[6] * 1e-3) / 1e12 if per_step[6] > 0 else 0.0
+    m2l_tf = m2l_flops / (per_step[5] * 1e-3) / 1e12 if per_step[5] > 0 else 0.0
     kernels = {
-        "p2p_l2p_integrate": {"ms": per_step[5], "tflops": p2p_tf, "flops_per_launch": p2p_flops, "launches": 1},
-        "traverse_m2l_l2l": {"ms": per_step[4], "tflops": trav_tf, "flops_per_step": m2l_flops,
-                             "launches": stats["depth"]},
+        "k_p2p": {"ms": per_step[6], "tflops": p2p_tf, "flops_per_launch": p2p_flops, "launches": 1,
+                  "phase": "near field + L2P + integrator"},
+        "k_m2l": {"ms": per_step[5], "tflops": m2l_tf, "flops_per_launch": m2l_flops, "launches": 1,
+                  "phase": "M2L (+ depth L2L launches, < 2 % of the phase)"},
     }
-    dom = "traverse_m2l_l2l" if per_step[4] >= per_step[5] else "p2p_l2p_integrate"
+    dom = "k_m2l" if per_step[5] >= per_step[6] else "k_p2p"
     ach = kernels[dom]["tflops"]
     roofline = {"bound": "fp32-pipe", "achieved": ach, "peak": fp32_peak_tf, "unit": "TFLOP/s",
                 "frac": ach / fp32_peak_tf if fp32_peak_tf else None, "traffic": None, "kernel": dom,
@@ -305,8 +307,7 @@ def main():
         "data": f"synthetic seeded collision ICs (seed {a.seed} + rank)", "config": workload_desc(a),
         "rms_force_err_vs_fp64_direct": rms_err, "max_force_err_vs_fp64_direct": max_err,
         "err_targets": int(len(tg)), "fwd_adjoint": None,
-        "phase_ms_per_step": {k: float(v) for k, v in zip(
-            ["kick_drift_keys", "sort_gather", "tree", "upward", "traverse_m2l_l2l", "p2p_l2p_integrate"], per_step)},
+        "phase_ms_per_step": {k: float(v) for k, v in zip(nb.CudaSimulation.PHASES, per_step)},
         "work_per_step": stats, "wall_s_timed": wall,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": a.n * 8 * 11, "d2h_bytes_per_step": a.n * 8 * 9,
                 "steps": a.e2e_steps},

@@ -164,9 +164,10 @@ int nbody_get_tree(nbody_ctx* c, uint64_t* keys, int64_t* perm, int32_t* nodes);
    computeInteractionBuffers (src/open_cl_simulation.cpp:176-369). */
 int nbody_get_interactions(nbody_ctx* c, int which, int64_t* npairs, int32_t* pairs);
 
-/* Per-phase device times (ms) of the last step: 0 kick/drift + keys, 1 sort +
-   gather, 2 tree, 3 upward pass, 4 traversal + M2L + L2L, 5 near field + L2P
-   + integration.  Timing is enabled by nbody_set_timing(c, 1). */
+/* Per-phase device times (ms) of the last force evaluation: 0 kick/drift +
+   keys, 1 sort + gather, 2 tree, 3 upward pass (P2M, M2M), 4 interaction
+   lists, 5 far field (M2L, L2L), 6 near field + L2P + integration.  Timing
+   is enabled by nbody_set_timing(c, 1). */
 int nbody_set_timing(nbody_ctx* c, int on);
 int nbody_phase_times(nbody_ctx* c, float* ms, int n);
 

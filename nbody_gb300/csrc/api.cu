@@ -183,9 +183,14 @@ int evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
     if (c->timing) cudaEventRecord(c->ev[2], c->st);
     NB_TRY(nb_build_tree(c));
     NB_TRY(fmm(c, integ, want_pot));
+    // error bits raised after the traversal check (asynchronous copies of the far field)
+    NB_CU(c, cudaMemcpyAsync(c->h_info, c->info.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->st));
+    NB_CU(c, cudaStreamSynchronize(c->st));
+    if ((uint32_t)c->h_info[INFO_ERR] & NB_ERRBIT_ASYNC)
+        return nb_fail(c, NBODY_ERR_CUDA, "a far-field copy did not complete in time");
     if (c->timing) {
-        NB_CU(c, cudaEventSynchronize(c->ev[6]));
-        for (int i = 0; i < 6; ++i) cudaEventElapsedTime(&c->phase_ms[i], c->ev[i], c->ev[i + 1]);
+        NB_CU(c, cudaEventSynchronize(c->ev[7]));
+        for (int i = 0; i < 7; ++i) cudaEventElapsedTime(&c->phase_ms[i], c->ev[i], c->ev[i + 1]);
     }
     return NBODY_OK;
 }
@@ -448,12 +453,6 @@ int nbody_get_tree(nbody_ctx* c, uint64_t* keys, int64_t* perm, int32_t* nodes) 
 int nbody_get_interactions(nbody_ctx* c, int which, int64_t* npairs, int32_t* pairs) {
     if (!c || !npairs || (which != 0 && which != 1)) return NBODY_ERR_INVALID;
     if (c->nnodes == 0) return nb_fail(c, NBODY_ERR_STATE, "no tree built yet");
-    if (which == 0 && !c->record_m2l) {
-        // far-field lists are evaluated on the fly; rebuild once with recording on
-        c->record_m2l = true;
-        int rc = nbody_compute_forces(c, nullptr, nullptr);
-        if (rc) { c->record_m2l = false; return rc; }
-    }
     NB_CU(c, cudaSetDevice(c->device));
     const int64_t nn = c->nnodes;
     std::vector<uint32_t> off(nn), cnt(nn);
@@ -480,7 +479,6 @@ int nbody_get_interactions(nbody_ctx* c, int which, int64_t* npairs, int32_t* pa
                 ++o;
             }
     }
-    if (which == 0) c->record_m2l = false;
     return NBODY_OK;
 }
 
@@ -492,7 +490,7 @@ int nbody_set_timing(nbody_ctx* c, int on) {
 
 int nbody_phase_times(nbody_ctx* c, float* ms, int n) {
     if (!c || !ms) return NBODY_ERR_INVALID;
-    for (int i = 0; i < n && i < 6; ++i) ms[i] = c->phase_ms[i];
+    for (int i = 0; i < n && i < 7; ++i) ms[i] = c->phase_ms[i];
     return NBODY_OK;
 }
 

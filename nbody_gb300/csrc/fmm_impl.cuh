@@ -8,14 +8,14 @@
 //               particle's offset from its leaf centre (packed with its charge);
 //   k_m2m       one tree level per launch, children shifted to the parent
 //               centre (translation offsets exact, in the shift precision);
-//   k_traverse  one tree level per launch: a warp per target cell refines its
+//   k_classify  one tree level per launch: a warp per target cell refines its
 //               parent's pending partners (src/interaction.cl:10-100 MAC and
-//               split rules), evaluates every accepted far-field partner at
-//               once (M2L into per-lane accumulators, no interaction buffer),
-//               writes the near-field and still-pending partners as one
-//               contiguous per-target list, and adds the parent's shifted
-//               local expansion (L2L).  Leaf targets descend remaining
-//               partners with a per-warp stack;
+//               split rules) into contiguous per-target far-field, near-field
+//               and pending lists; leaf targets descend remaining partners
+//               with a per-warp stack;
+//   k_m2l       every cell's far-field list at once (M2L into per-lane
+//               partial expansions, fixed-order reduction);
+//   k_l2l       one level per launch, parent's local expansion shifted down;
 //   k_p2p       a warp per leaf: near-field sums over its partner leaves with
 //               source tiles staged in shared memory, the local expansion
 //               evaluated at each particle (L2P), and the integrator update as
@@ -40,7 +40,6 @@ template <> struct Prec<NBODY_PREC_FP32> {
     typedef float H;   // expansions and shifts (M2M, L2L)
     typedef float4 S4;
     static constexpr bool kahan = false;
-    static constexpr int trav_warps = 8;
     static constexpr bool lane_smem = false;
 };
 template <> struct Prec<NBODY_PREC_MIXED> {
@@ -49,7 +48,6 @@ template <> struct Prec<NBODY_PREC_MIXED> {
     typedef double H;
     typedef float4 S4;
     static constexpr bool kahan = true;
-    static constexpr int trav_warps = 8;
     static constexpr bool lane_smem = false;
 };
 template <> struct Prec<NBODY_PREC_FP64> {
@@ -58,8 +56,7 @@ template <> struct Prec<NBODY_PREC_FP64> {
     typedef double H;
     typedef D4 S4;
     static constexpr bool kahan = false;
-    static constexpr int trav_warps = 1;
-    static constexpr bool lane_smem = true;   // per-lane D and L live in shared memory
+    static constexpr bool lane_smem = true;   // per-lane M2L arrays live in shared memory
 };
 
 constexpr int STK = 512;         // descent stack entries per warp
@@ -112,6 +109,7 @@ __global__ void __launch_bounds__(128) k_p2m(int64_t nleaves, const uint32_t* __
     typedef typename Prec<MODE>::S S;
     typedef typename Prec<MODE>::H H;
     constexpr int T = nb_terms<P>::value;
+    constexpr int TM = nb_tm<P>::value;
     __shared__ S pw[4][32][3][P + 1];
     __shared__ S qq[4][32];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
@@ -166,8 +164,8 @@ __global__ void __launch_bounds__(128) k_p2m(int64_t nleaves, const uint32_t* __
         int a = lane + 32 * j;
         if (a < T) {
             H v = (H)acc[j] * (H)nb_invfact[a];
-            M[(int64_t)k * T + a] = v;
-            if (M32) M32[(int64_t)k * T + a] = (float)v;
+            M[(int64_t)k * TM + a] = v;
+            if (M32) M32[(int64_t)k * TM + a] = (float)v;
         }
     }
 }
@@ -181,6 +179,7 @@ __global__ void __launch_bounds__(128) k_m2m(int lo, int hi, const NodeRec* __re
                                              float* __restrict__ M32) {
     typedef typename Prec<MODE>::H H;
     constexpr int T = nb_terms<P>::value;
+    constexpr int TM = nb_tm<P>::value;
     __shared__ H sM[4][T];
     __shared__ H sY[4][T];
     __shared__ H spw[4][3][P + 1];
@@ -201,7 +200,7 @@ __global__ void __launch_bounds__(128) k_m2m(int lo, int hi, const NodeRec* __re
         const NodeRec cn = nodes[ch];
         double dx, dy, dz;
         disp(cn, nd, unit, dx, dy, dz);
-        for (int a = lane; a < T; a += 32) sM[wib][a] = M[(int64_t)ch * T + a];
+        for (int a = lane; a < T; a += 32) sM[wib][a] = M[(int64_t)ch * TM + a];
         if (lane < 3) {
             H d = (H)(lane == 0 ? dx : lane == 1 ? dy : dz), p = H(1);
             for (int e = 0; e <= P; ++e) { spw[wib][lane][e] = p; p *= d; }
@@ -226,21 +225,29 @@ __global__ void __launch_bounds__(128) k_m2m(int lo, int hi, const NodeRec* __re
     for (int j = 0; j < NPL; ++j) {
         int a = lane + 32 * j;
         if (a < T) {
-            M[(int64_t)k * T + a] = acc[j];
-            if (M32) M32[(int64_t)k * T + a] = (float)acc[j];
+            M[(int64_t)k * TM + a] = acc[j];
+            if (M32) M32[(int64_t)k * TM + a] = (float)acc[j];
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// traversal round 0: the root
+// far field, part 1: interaction lists, one tree level per launch
+//
+// A warp per target cell t of the level refines the pending partners of its
+// parent (src/interaction.cl:10-100 split rules, reorganised per target):
+// each candidate s is a child of a pending partner, or the partner itself if
+// it is a leaf.  s is accepted for the far field when the MAC holds
+// (src/interaction.cl:64-79), kept as a near-field partner when both are
+// leaves, kept pending when t has children, and otherwise (t a leaf, s not)
+// descended with a per-warp stack.  Two passes: the first counts, one
+// atomicAdd per list reserves a contiguous block per target, the second
+// writes in the same order.
 // ---------------------------------------------------------------------------
 template <int MODE, int P>
-__global__ void k_root(const NodeRec* __restrict__ nodes, typename Prec<MODE>::H* __restrict__ L,
-                       uint32_t* pend_off, uint32_t* pend_cnt, uint32_t* pend_list, uint32_t* p2p_off,
-                       uint32_t* p2p_cnt, uint32_t* p2p_list, int32_t* info) {
-    constexpr int T = nb_terms<P>::value;
-    for (int a = threadIdx.x; a < T; a += blockDim.x) L[a] = 0;
+__global__ void k_root(const NodeRec* __restrict__ nodes, uint32_t* pend_off, uint32_t* pend_cnt,
+                       uint32_t* pend_list, uint32_t* p2p_off, uint32_t* p2p_cnt, uint32_t* p2p_list,
+                       uint32_t* m2l_off, uint32_t* m2l_cnt, int32_t* info) {
     if (threadIdx.x == 0) {
         const bool leaf = nodes[0].nchild == 0;
         uint32_t* tail = (uint32_t*)&info[leaf ? INFO_P2P_TAIL : INFO_PEND_TAIL];
@@ -248,145 +255,98 @@ __global__ void k_root(const NodeRec* __restrict__ nodes, typename Prec<MODE>::H
         *tail = o + 1;
         if (leaf) { p2p_list[o] = 0; p2p_off[0] = o; p2p_cnt[0] = 1; pend_cnt[0] = 0; }
         else { pend_list[o] = 0; pend_off[0] = o; pend_cnt[0] = 1; p2p_cnt[0] = 0; }
+        m2l_off[0] = 0;
+        m2l_cnt[0] = 0;
     }
 }
 
-struct TravArgs {
+struct ClassArgs {
     const NodeRec* nodes;
-    const BoxDev* box;
-    const void* Mm2l;       // S*: multipoles read by M2L
-    void* L;                // H*
-    uint32_t *pend_off, *pend_cnt, *pend_list, *p2p_off, *p2p_cnt, *p2p_list;
-    uint32_t pend_cap, p2p_cap;
-    uint32_t *m2l_off, *m2l_cnt, *m2l_list;   // null unless the far-field lists are recorded
-    uint32_t m2l_cap;
-    unsigned long long* stats;                // [0] M2L pairs, [1] P2P particle pairs, [2] P2P leaf pairs
+    uint32_t *pend_off, *pend_cnt, *pend_list, *p2p_off, *p2p_cnt, *p2p_list, *m2l_off, *m2l_cnt, *m2l_list;
+    uint32_t pend_cap, p2p_cap, m2l_cap;
+    unsigned long long* stats;   // [0] M2L pairs, [1] P2P particle pairs, [2] P2P leaf pairs
     int32_t* info;
-    double theta2x4;        // 4 theta^2
-    double eps2;
-    int lo, hi;             // target node range (one level)
+    float theta2;                // theta^2 formed in FP32, as the reference does
+    int lo, hi;                  // target node range (one level)
 };
 
-template <int MODE, int P>
-struct TravSmem {
-    typedef typename Prec<MODE>::H H;
-    static constexpr int T = nb_terms<P>::value;
-    static constexpr size_t lane_arrays =
-        Prec<MODE>::lane_smem ? (size_t)2 * 32 * T * sizeof(typename Prec<MODE>::S) : 0;
-    static constexpr size_t per_warp_raw =
-        sizeof(uint32_t) * (CAND + STK + 64) + sizeof(H) * (3 * T + 3 * (P + 1)) + lane_arrays;
-    static constexpr size_t per_warp = (per_warp_raw + 255) / 256 * 256;
-};
+// centre (2i+1) << (21 - level) in fine units (side / 2^22); fits in 32 bits
+__device__ __forceinline__ void centre_fine32(const NodeRec& nd, int& cx, int& cy, int& cz) {
+    const int sh = NB_LEVELS - nd.level;
+    cx = (int)((2u * nd.ix + 1u) << sh);
+    cy = (int)((2u * nd.iy + 1u) << sh);
+    cz = (int)((2u * nd.iz + 1u) << sh);
+}
 
-template <int MODE, int P>
-__global__ void __launch_bounds__(32 * Prec<MODE>::trav_warps, 1) k_traverse(TravArgs A) {
-    typedef typename Prec<MODE>::S S;
-    typedef typename Prec<MODE>::H H;
-    constexpr int T = nb_terms<P>::value;
-    constexpr bool LS = Prec<MODE>::lane_smem;
-    extern __shared__ __align__(256) unsigned char smem_raw[];
+// MAC of src/interaction.cl:64-79 in its own FP32 operation order: displacement of centres,
+// distance^2 = ((x*x + y*y) + z*z) + w*w with w = 0, extent^2 = (0.75 * (wA+wB)) * (wA+wB),
+// approximate iff extent^2 / distance^2 < theta^2.  Lengths are in fine units, an exact
+// power-of-two rescaling of the reference's box units, so every rounding is the reference's.
+__device__ __forceinline__ bool mac_f32(int tcx, int tcy, int tcz, float tw, const NodeRec& s, float theta2) {
+    int sx, sy, sz;
+    centre_fine32(s, sx, sy, sz);
+    const float dx = (float)(sx - tcx), dy = (float)(sy - tcy), dz = (float)(sz - tcz);
+    const float d2 = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)), 0.0f);
+    const float es = __fadd_rn(tw, (float)(1u << (NB_LEVELS + 1 - s.level)));
+    const float e2 = __fmul_rn(__fmul_rn(0.75f, es), es);
+    return __fdiv_rn(e2, d2) < theta2;
+}
+
+constexpr int CLS_WARPS = 8;
+
+static __global__ void __launch_bounds__(32 * CLS_WARPS) k_classify(ClassArgs A) {
+    __shared__ uint32_t s_cand[CLS_WARPS][CAND];
+    __shared__ uint32_t s_stk[CLS_WARPS][STK];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const int t = A.lo + blockIdx.x * Prec<MODE>::trav_warps + wib;
+    const int t = A.lo + blockIdx.x * CLS_WARPS + wib;
     if (t >= A.hi) return;
-    unsigned char* ws = smem_raw + (size_t)wib * TravSmem<MODE, P>::per_warp;
-    uint32_t* cand = (uint32_t*)ws;
-    uint32_t* stk = cand + CAND;
-    uint32_t* batch = stk + STK;
-    H* sLp = (H*)(batch + 64);
-    H* sY = sLp + T;
-    H* sLs = sY + T;
-    H* spw = sLs + T;
-    S* laneD = (S*)(spw + 3 * (P + 1));
-    S* laneL = laneD + 32 * T;
-
+    uint32_t* cand = s_cand[wib];
+    uint32_t* stk = s_stk[wib];
     const NodeRec nt = A.nodes[t];
     const bool tleaf = nt.nchild == 0;
-    long long tcx, tcy, tcz;
-    nb_centre_fine(nt, tcx, tcy, tcz);
-    const long long tw = nb_width_fine(nt);
-    const double unit = A.box->unit;
+    int tcx, tcy, tcz;
+    centre_fine32(nt, tcx, tcy, tcz);
+    const float tw = (float)(1u << (NB_LEVELS + 1 - nt.level));
     const int par = nt.parent;
     const uint32_t pb = A.pend_off[par], pc = A.pend_cnt[par];
-    const S* Msrc = (const S*)A.Mm2l;
-
-    // per-lane partial local expansion: registers (FP32 forms) or a shared-memory column (FP64)
-    S Lreg[LS ? 1 : T];
-    if constexpr (LS) {
-        for (int a = 0; a < T; ++a) laneL[a * 32 + lane] = S(0);
-    } else {
-#pragma unroll
-        for (int a = 0; a < T; ++a) Lreg[a] = S(0);
-    }
-
-    uint32_t out_base = 0, n_out = 0, m_base = 0, m_pos = 0, n_apx = 0;
-    unsigned long long src_particles = 0;     // per lane: particles of near-field partners (write pass)
-    bool can_write = false, m_write = false;
-    int bn = 0;
     uint32_t* out_list = tleaf ? A.p2p_list : A.pend_list;
-
-    auto m2l_batch = [&](int cnt) {
-        if (lane < cnt) {
-            const uint32_t s = batch[lane];
-            const NodeRec sn = A.nodes[s];
-            long long sx, sy, sz;
-            nb_centre_fine(sn, sx, sy, sz);
-            const S dx = (S)((double)(tcx - sx) * unit), dy = (S)((double)(tcy - sy) * unit),
-                    dz = (S)((double)(tcz - sz) * unit);
-            if constexpr (LS) {
-                Ops<S, P>::template derivs<32>(dx, dy, dz, (S)A.eps2, laneD + lane);
-                Ops<S, P>::template m2l<32>(Msrc + (int64_t)s * T, laneD + lane, laneL + lane);
-            } else {
-                S D[T];
-                Ops<S, P>::template derivs<1>(dx, dy, dz, (S)A.eps2, D);
-                Ops<S, P>::template m2l<1>(Msrc + (int64_t)s * T, D, Lreg);
-            }
-        }
-    };
+    uint32_t out_base = 0, n_out = 0, m_base = 0, n_apx = 0;
+    bool can_write = false, m_write = false;
+    unsigned long long src_particles = 0;
 
     for (int pass = 0; pass < 2; ++pass) {
-        uint32_t wpos = 0;
+        uint32_t wpos = 0, mpos = 0;
         int top = 0;
-        m_pos = 0;
         auto classify = [&](uint32_t s) {
             const bool valid = s != NONE;
             NodeRec sn;
+            sn.nchild = 0;
+            sn.count = 0;
             if (valid) sn = A.nodes[s];
-            const bool approx = valid && (int)s != t && mac_accept(tcx, tcy, tcz, tw, sn, A.theta2x4);
+            const bool approx = valid && (int)s != t && mac_f32(tcx, tcy, tcz, tw, sn, A.theta2);
             const bool sleaf = valid && sn.nchild == 0;
             const bool out = valid && !approx && (!tleaf || sleaf);
             const bool desc = valid && !approx && tleaf && !sleaf;
             const uint32_t mo = __ballot_sync(0xffffffffu, out);
             if (out && pass == 1 && can_write) {
-                uint32_t pos = wpos + __popc(mo & lanemask_lt());
+                const uint32_t pos = wpos + __popc(mo & lanemask_lt());
                 if (pos < n_out) out_list[out_base + pos] = s;
                 if (tleaf) src_particles += sn.count;
             }
             wpos += __popc(mo);
+            const uint32_t ma = __ballot_sync(0xffffffffu, approx);
+            if (approx && pass == 1 && m_write) {
+                const uint32_t pos = mpos + __popc(ma & lanemask_lt());
+                if (pos < n_apx) A.m2l_list[m_base + pos] = s;
+            }
+            mpos += __popc(ma);
             const uint32_t md = __ballot_sync(0xffffffffu, desc);
             if (desc) {
-                int pos = top + __popc(md & lanemask_lt());
+                const int pos = top + __popc(md & lanemask_lt());
                 if (pos < STK) stk[pos] = s;
                 else atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_STACK);
             }
             top = min(top + __popc(md), STK);
-            const uint32_t ma = __ballot_sync(0xffffffffu, approx);
-            if (A.m2l_list) {
-                if (pass == 1 && approx && m_write) A.m2l_list[m_base + m_pos + __popc(ma & lanemask_lt())] = s;
-                m_pos += __popc(ma);
-            }
-            if (pass == 1) {
-                n_apx += __popc(ma);
-                if (approx) batch[bn + __popc(ma & lanemask_lt())] = s;
-                bn += __popc(ma);
-                __syncwarp();
-                if (bn >= 32) {
-                    m2l_batch(32);
-                    __syncwarp();
-                    if (lane < bn - 32) batch[lane] = batch[32 + lane];
-                    bn -= 32;
-                    __syncwarp();
-                }
-            }
         };
         auto drain_stack = [&]() {
             while (top > 0) {
@@ -430,44 +390,34 @@ __global__ void __launch_bounds__(32 * Prec<MODE>::trav_warps, 1) k_traverse(Tra
         }
         if (pass == 0) {
             n_out = wpos;
-            uint32_t base = 0;
-            int ok = 0;
+            n_apx = mpos;
+            uint32_t base = 0, mb = 0;
+            int ok = 0, mok = 0;
             if (lane == 0) {
                 uint32_t* tail = (uint32_t*)&A.info[tleaf ? INFO_P2P_TAIL : INFO_PEND_TAIL];
                 const uint32_t cap = tleaf ? A.p2p_cap : A.pend_cap;
                 base = atomicAdd(tail, n_out);
                 ok = (uint64_t)base + n_out <= cap;
                 if (!ok) atomicOr((unsigned int*)&A.info[INFO_ERR], tleaf ? NB_ERRBIT_P2P_CAP : NB_ERRBIT_PEND_CAP);
+                mb = atomicAdd((uint32_t*)&A.info[INFO_M2L_TAIL], n_apx);
+                mok = (uint64_t)mb + n_apx <= A.m2l_cap;
+                if (!mok) atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_M2L_CAP);
+                if (tleaf) {
+                    A.p2p_off[t] = base; A.p2p_cnt[t] = ok ? n_out : 0;
+                    A.pend_cnt[t] = 0;
+                } else {
+                    A.pend_off[t] = base; A.pend_cnt[t] = ok ? n_out : 0;
+                    A.p2p_cnt[t] = 0;
+                }
+                A.m2l_off[t] = mb;
+                A.m2l_cnt[t] = mok ? n_apx : 0;
             }
             out_base = __shfl_sync(0xffffffffu, base, 0);
             can_write = __shfl_sync(0xffffffffu, ok, 0);
-            if (A.m2l_list) {
-                uint32_t mb = 0;
-                int mok = 0;
-                if (lane == 0) {
-                    mb = atomicAdd((uint32_t*)&A.info[INFO_M2L_TAIL], m_pos);
-                    mok = (uint64_t)mb + m_pos <= A.m2l_cap;
-                    if (!mok) atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_M2L_CAP);
-                    A.m2l_off[t] = mb;
-                    A.m2l_cnt[t] = mok ? m_pos : 0;
-                }
-                m_base = __shfl_sync(0xffffffffu, mb, 0);
-                m_write = __shfl_sync(0xffffffffu, mok, 0);
-            }
-            if (lane == 0) {
-                if (tleaf) {
-                    A.p2p_off[t] = out_base; A.p2p_cnt[t] = can_write ? n_out : 0;
-                    A.pend_cnt[t] = 0;
-                } else {
-                    A.pend_off[t] = out_base; A.pend_cnt[t] = can_write ? n_out : 0;
-                    A.p2p_cnt[t] = 0;
-                }
-            }
+            m_base = __shfl_sync(0xffffffffu, mb, 0);
+            m_write = __shfl_sync(0xffffffffu, mok, 0);
         }
     }
-    __syncwarp();
-    if (bn > 0) m2l_batch(bn);
-    __syncwarp();
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) src_particles += __shfl_xor_sync(0xffffffffu, src_particles, o);
     if (lane == 0) {
@@ -477,8 +427,168 @@ __global__ void __launch_bounds__(32 * Prec<MODE>::trav_warps, 1) k_traverse(Tra
             atomicAdd(&A.stats[2], (unsigned long long)n_out);
         }
     }
+}
 
-    // reduce the per-lane partial local expansions (fixed butterfly order)
+// ---------------------------------------------------------------------------
+// far field, part 2: M2L over every cell at once
+//
+// A warp per target; lanes take 32 list entries at a time, each computing the
+// derivative tensor of its own displacement and contracting it with its
+// source's multipoles into a per-lane partial local expansion; the partials
+// are reduced in a fixed butterfly order.  The 32 multipole rows of a batch
+// are brought into shared memory by TMA bulk copies (one cp.async.bulk per
+// lane, completing on the stage's mbarrier) while the previous batch is
+// being computed: two stages, every wait bounded in time.  Row stride in
+// shared memory makes the per-lane 16-byte reads conflict free.
+// Displacements are exact: 32-bit fine-unit offsets times the fine unit.
+// ---------------------------------------------------------------------------
+struct M2LArgs {
+    const NodeRec* nodes;
+    const BoxDev* box;
+    const void* Mm2l;        // S*: multipoles read by M2L, row stride nb_tm<P>
+    void* L;                 // H*: receives the M2L sum of each target
+    const uint32_t *m2l_off, *m2l_cnt, *m2l_list;
+    int32_t* info;
+    double eps2;
+    int64_t nnodes;
+};
+
+template <int MODE, int P>
+struct M2LSmem {
+    typedef typename Prec<MODE>::S S;
+    static constexpr int T = nb_terms<P>::value;
+    static constexpr int TM = nb_tm<P>::value;
+    // 16-byte chunks per shared row must be odd: the 8 lanes of a quarter warp then read 8 distinct bank groups
+    static constexpr int SST = sizeof(S) == 4 ? ((TM / 4) % 2 ? TM : TM + 4) : TM + 2;
+    static constexpr int warps = Prec<MODE>::lane_smem ? 1 : 4;
+    static constexpr size_t rows = (size_t)2 * 32 * SST * sizeof(S);
+    static constexpr size_t lane_arrays = Prec<MODE>::lane_smem ? (size_t)2 * 32 * T * sizeof(S) : 0;
+    static constexpr size_t per_warp = (16 + rows + lane_arrays + 255) / 256 * 256;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// warp-uniform bounded wait (about a second at GB300 clocks); false on timeout
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity) {
+    const long long t0 = clock64();
+    bool ok = false;
+    for (;;) {
+        ok = ok || mbar_try_wait(bar, parity);
+        if (__all_sync(0xffffffffu, ok)) return true;
+        const long long dt = __shfl_sync(0xffffffffu, clock64() - t0, 0);
+        if (dt > 2000000000ll) return false;
+    }
+}
+
+template <int MODE, int P>
+__global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A) {
+    typedef typename Prec<MODE>::S S;
+    typedef typename Prec<MODE>::H H;
+    constexpr int T = nb_terms<P>::value;
+    constexpr int TM = nb_tm<P>::value;
+    constexpr int SST = M2LSmem<MODE, P>::SST;
+    constexpr bool LS = Prec<MODE>::lane_smem;
+    constexpr int W = M2LSmem<MODE, P>::warps;
+    constexpr uint32_t ROWB = TM * sizeof(S);
+    extern __shared__ __align__(256) unsigned char smem_raw[];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int64_t t = (int64_t)blockIdx.x * W + wib;
+    if (t >= A.nnodes) return;
+    unsigned char* ws = smem_raw + (size_t)wib * M2LSmem<MODE, P>::per_warp;
+    uint64_t* bar = (uint64_t*)ws;
+    S* rows = (S*)(ws + 16);
+    S* laneD = rows + 2 * 32 * SST;
+    S* laneL = laneD + 32 * T;
+    const NodeRec nt = A.nodes[t];
+    int tcx, tcy, tcz;
+    centre_fine32(nt, tcx, tcy, tcz);
+    const S unit = (S)A.box->unit;
+    const S eps2 = (S)A.eps2;
+    const S* Msrc = (const S*)A.Mm2l;
+    const uint32_t off = A.m2l_off[t], cnt = A.m2l_cnt[t];
+    const uint32_t nbatch = (cnt + 31) / 32;
+    S Lreg[LS ? 1 : T];
+    if constexpr (LS) {
+        for (int a = 0; a < T; ++a) laneL[a * 32 + lane] = S(0);
+    } else {
+#pragma unroll
+        for (int a = 0; a < T; ++a) Lreg[a] = S(0);
+    }
+    if (lane == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    // issue the bulk copies of batch b into stage b & 1; returns this lane's source
+    auto issue = [&](uint32_t b) -> uint32_t {
+        const uint32_t nb = min(32u, cnt - 32 * b);
+        const uint32_t k = b & 1;
+        const uint32_t s = (uint32_t)lane < nb ? A.m2l_list[off + 32 * b + lane] : 0u;
+        fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) mbar_expect_tx(&bar[k], nb * ROWB);
+        __syncwarp();
+        if ((uint32_t)lane < nb) bulk_g2s(rows + (k * 32 + lane) * SST, Msrc + (int64_t)s * TM, ROWB, &bar[k]);
+        return s;
+    };
+    bool failed = false;
+    uint32_t b_fail = 0;
+    uint32_t s_next = nbatch ? issue(0) : 0u;
+    for (uint32_t b = 0; b < nbatch; ++b) {
+        const uint32_t s_cur = s_next;
+        const uint32_t k = b & 1;
+        const uint32_t nb = min(32u, cnt - 32 * b);
+        if (b + 1 < nbatch) s_next = issue(b + 1);
+        if (!mbar_wait_warp(&bar[k], (b >> 1) & 1)) { failed = true; b_fail = b; break; }
+        if ((uint32_t)lane < nb) {
+            const NodeRec sn = A.nodes[s_cur];
+            int sx, sy, sz;
+            centre_fine32(sn, sx, sy, sz);
+            const S dx = (S)(tcx - sx) * unit, dy = (S)(tcy - sy) * unit, dz = (S)(tcz - sz) * unit;
+            const S* row = rows + (k * 32 + lane) * SST;
+            if constexpr (LS) {
+                Ops<S, P>::template derivs<32>(dx, dy, dz, eps2, laneD + lane);
+                Ops<S, P>::template m2l_v<32>(row, laneD + lane, laneL + lane);
+            } else {
+                S D[T];
+                Ops<S, P>::template derivs<1>(dx, dy, dz, eps2, D);
+                Ops<S, P>::template m2l_v<1>(row, D, Lreg);
+            }
+        }
+        __syncwarp();
+    }
+    if (failed) {
+        // let every copy already issued land before the shared memory is released
+        if (lane == 0) atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_ASYNC);
+        mbar_wait_warp(&bar[b_fail & 1], (b_fail >> 1) & 1);
+        if (b_fail + 1 < nbatch) mbar_wait_warp(&bar[(b_fail + 1) & 1], ((b_fail + 1) >> 1) & 1);
+        return;
+    }
+    H* Lg = (H*)A.L;
 #pragma unroll
     for (int a = 0; a < T; ++a) {
         S v;
@@ -486,28 +596,47 @@ __global__ void __launch_bounds__(32 * Prec<MODE>::trav_warps, 1) k_traverse(Tra
         else v = Lreg[a];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += shfl_xor_t(v, o);
-        if ((a & 31) == lane) sLs[a] = (H)v;
+        if ((a & 31) == lane) Lg[t * T + a] = (H)v;
     }
-    // L2L from the parent + store
-    const NodeRec pn = A.nodes[par];
+}
+
+// ---------------------------------------------------------------------------
+// far field, part 3: L2L, one level per launch (top down), warp per cell:
+// L(t) = M2L sum of t + parent's L shifted to t's centre (exact FP64 offset
+// in the mixed and FP64 forms).
+// ---------------------------------------------------------------------------
+template <int MODE, int P>
+__global__ void __launch_bounds__(128) k_l2l(int lo, int hi, const NodeRec* __restrict__ nodes,
+                                             const BoxDev* __restrict__ boxp, typename Prec<MODE>::H* __restrict__ L) {
+    typedef typename Prec<MODE>::H H;
+    constexpr int T = nb_terms<P>::value;
+    __shared__ H sLp[4][T];
+    __shared__ H sY[4][T];
+    __shared__ H spw[4][3][P + 1];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int t = lo + blockIdx.x * 4 + wib;
+    if (t >= hi) return;
+    const NodeRec nt = nodes[t];
+    const int par = nt.parent;
+    const NodeRec pn = nodes[par];
     double dx, dy, dz;
-    disp(nt, pn, unit, dx, dy, dz);
-    H* Lg = (H*)A.L;
-    for (int a = lane; a < T; a += 32) sLp[a] = Lg[(int64_t)par * T + a];
+    disp(nt, pn, boxp->unit, dx, dy, dz);
+    for (int a = lane; a < T; a += 32) sLp[wib][a] = L[(int64_t)par * T + a];
     if (lane < 3) {
         H d = (H)(lane == 0 ? dx : lane == 1 ? dy : dz), p = H(1);
-        for (int e = 0; e <= P; ++e) { spw[lane * (P + 1) + e] = p; p *= d; }
+        for (int e = 0; e <= P; ++e) { spw[wib][lane][e] = p; p *= d; }
     }
     __syncwarp();
     for (int a = lane; a < T; a += 32)
-        sY[a] = spw[nb_mi[a][0]] * spw[(P + 1) + nb_mi[a][1]] * spw[2 * (P + 1) + nb_mi[a][2]] * (H)nb_invfact[a];
+        sY[wib][a] = spw[wib][0][nb_mi[a][0]] * spw[wib][1][nb_mi[a][1]] * spw[wib][2][nb_mi[a][2]] *
+                     (H)nb_invfact[a];
     __syncwarp();
     const unsigned short* st = Tabs<P>::l2l_start();
     const unsigned short* pr = Tabs<P>::l2l_pairs();
     for (int a = lane; a < T; a += 32) {
-        H s = sLs[a];
-        for (int u = st[a]; u < st[a + 1]; ++u) s = nb_fma(sLp[pr[2 * u]], sY[pr[2 * u + 1]], s);
-        Lg[(int64_t)t * T + a] = s;
+        H v = L[(int64_t)t * T + a];
+        for (int u = st[a]; u < st[a + 1]; ++u) v = nb_fma(sLp[wib][pr[2 * u]], sY[wib][pr[2 * u + 1]], v);
+        L[(int64_t)t * T + a] = v;
     }
 }
 
@@ -791,8 +920,9 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     constexpr int T = nb_terms<P>::value;
     const int64_t nn = c->nnodes, n = c->n;
     const int cur = c->cur;
-    NB_TRY(nb_grow(c, c->M, sizeof(H) * T * nn));
-    if (MODE == NBODY_PREC_MIXED) NB_TRY(nb_grow(c, c->M32, sizeof(float) * T * nn));
+    constexpr int TM = nb_tm<P>::value;
+    NB_TRY(nb_grow(c, c->M, sizeof(H) * TM * nn));
+    if (MODE == NBODY_PREC_MIXED) NB_TRY(nb_grow(c, c->M32, sizeof(float) * TM * nn));
     NB_TRY(nb_grow(c, c->L, sizeof(H) * T * nn));
     NB_TRY(nb_grow(c, c->src, sizeof(S4) * n));
     NB_TRY(nb_grow(c, c->pend_off, sizeof(uint32_t) * nn));
@@ -818,59 +948,51 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     }
     if (c->timing) cudaEventRecord(c->ev[4], c->st);
 
-    const size_t smem = (size_t)Prec<MODE>::trav_warps * TravSmem<MODE, P>::per_warp;
-    NB_CU(c, cudaFuncSetAttribute(k_traverse<MODE, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    NB_TRY(nb_grow(c, c->m2l_off, sizeof(uint32_t) * nn));
+    NB_TRY(nb_grow(c, c->m2l_cnt, sizeof(uint32_t) * nn));
     for (int attempt = 0; attempt < 8; ++attempt) {
         size_t want_pend = (size_t)64 * nn + 1024, want_p2p = (size_t)96 * c->nleaves + 1024;
+        size_t want_m2l = (size_t)512 * nn + 1024;
         if (c->pend_cap < want_pend) c->pend_cap = want_pend;
         if (c->p2p_cap < want_p2p) c->p2p_cap = want_p2p;
+        if (c->m2l_cap < want_m2l) c->m2l_cap = want_m2l;
+        c->pend_cap = std::min<size_t>(c->pend_cap, 0xffffffffu);
+        c->p2p_cap = std::min<size_t>(c->p2p_cap, 0xffffffffu);
+        c->m2l_cap = std::min<size_t>(c->m2l_cap, 0xffffffffu);
         NB_TRY(nb_grow(c, c->pend_list, sizeof(uint32_t) * c->pend_cap));
         NB_TRY(nb_grow(c, c->p2p_list, sizeof(uint32_t) * c->p2p_cap));
-        if (c->record_m2l) {
-            size_t want_m2l = (size_t)256 * nn + 1024;
-            if (c->m2l_cap < want_m2l) c->m2l_cap = want_m2l;
-            NB_TRY(nb_grow(c, c->m2l_list, sizeof(uint32_t) * c->m2l_cap));
-            NB_TRY(nb_grow(c, c->m2l_off, sizeof(uint32_t) * nn));
-            NB_TRY(nb_grow(c, c->m2l_cnt, sizeof(uint32_t) * nn));
-            NB_CU(c, cudaMemsetAsync(c->m2l_cnt.p, 0, sizeof(uint32_t) * nn, c->st));
-        }
+        NB_TRY(nb_grow(c, c->m2l_list, sizeof(uint32_t) * c->m2l_cap));
         int32_t* info = DP<int32_t>(c->info);
         NB_TRY(nb_grow(c, c->stats, 8 * sizeof(unsigned long long)));
         NB_CU(c, cudaMemsetAsync(c->stats.p, 0, 8 * sizeof(unsigned long long), c->st));
         NB_CU(c, cudaMemsetAsync(info + INFO_PEND_TAIL, 0, 3 * sizeof(int32_t), c->st));
         NB_CU(c, cudaMemsetAsync(info + INFO_ERR, 0, sizeof(int32_t), c->st));
-        k_root<MODE, P><<<1, 32, 0, c->st>>>(DP<NodeRec>(c->nodes), DP<H>(c->L), DP<uint32_t>(c->pend_off),
+        k_root<MODE, P><<<1, 32, 0, c->st>>>(DP<NodeRec>(c->nodes), DP<uint32_t>(c->pend_off),
                                              DP<uint32_t>(c->pend_cnt), DP<uint32_t>(c->pend_list),
                                              DP<uint32_t>(c->p2p_off), DP<uint32_t>(c->p2p_cnt),
-                                             DP<uint32_t>(c->p2p_list), info);
+                                             DP<uint32_t>(c->p2p_list), DP<uint32_t>(c->m2l_off),
+                                             DP<uint32_t>(c->m2l_cnt), info);
         NB_LAUNCHED(c, "root");
         c->launches += 1;
-        TravArgs A;
+        ClassArgs A;
         A.nodes = DP<NodeRec>(c->nodes);
-        A.box = box;
-        A.Mm2l = MODE == NBODY_PREC_MIXED ? (const void*)M32 : (const void*)c->M.p;
-        A.L = c->L.p;
         A.pend_off = DP<uint32_t>(c->pend_off); A.pend_cnt = DP<uint32_t>(c->pend_cnt);
         A.pend_list = DP<uint32_t>(c->pend_list);
         A.p2p_off = DP<uint32_t>(c->p2p_off); A.p2p_cnt = DP<uint32_t>(c->p2p_cnt);
         A.p2p_list = DP<uint32_t>(c->p2p_list);
-        A.pend_cap = (uint32_t)c->pend_cap; A.p2p_cap = (uint32_t)c->p2p_cap;
-        A.m2l_list = c->record_m2l ? DP<uint32_t>(c->m2l_list) : nullptr;
-        A.m2l_off = c->record_m2l ? DP<uint32_t>(c->m2l_off) : nullptr;
-        A.m2l_cnt = c->record_m2l ? DP<uint32_t>(c->m2l_cnt) : nullptr;
-        A.m2l_cap = (uint32_t)c->m2l_cap;
+        A.m2l_off = DP<uint32_t>(c->m2l_off); A.m2l_cnt = DP<uint32_t>(c->m2l_cnt);
+        A.m2l_list = DP<uint32_t>(c->m2l_list);
+        A.pend_cap = (uint32_t)c->pend_cap; A.p2p_cap = (uint32_t)c->p2p_cap; A.m2l_cap = (uint32_t)c->m2l_cap;
         A.stats = DP<unsigned long long>(c->stats);
         A.info = info;
         const float th = (float)c->prm.theta;
-        A.theta2x4 = 4.0 * (double)(th * th);
-        A.eps2 = c->prm.eps * c->prm.eps;
+        A.theta2 = th * th;
         for (int r = 1; r <= c->depth; ++r) {
             A.lo = c->level_start[r];
             A.hi = c->level_start[r + 1];
             if (A.hi <= A.lo) continue;
-            const int W = Prec<MODE>::trav_warps;
-            k_traverse<MODE, P><<<(unsigned)((A.hi - A.lo + W - 1) / W), 32 * W, smem, c->st>>>(A);
-            NB_LAUNCHED(c, "traverse");
+            k_classify<<<(unsigned)((A.hi - A.lo + CLS_WARPS - 1) / CLS_WARPS), 32 * CLS_WARPS, 0, c->st>>>(A);
+            NB_LAUNCHED(c, "classify");
             c->launches += 1;
         }
         // near-field work plan: chunks per leaf and partial-sum slots, scanned
@@ -906,6 +1028,33 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
         if (attempt == 7) return nb_fail(c, NBODY_ERR_CAPACITY, "interaction lists kept overflowing");
     }
     if (c->timing) cudaEventRecord(c->ev[5], c->st);
+    {
+        M2LArgs B;
+        B.nodes = DP<NodeRec>(c->nodes);
+        B.box = box;
+        B.Mm2l = MODE == NBODY_PREC_MIXED ? (const void*)M32 : (const void*)c->M.p;
+        B.L = c->L.p;
+        B.m2l_off = DP<uint32_t>(c->m2l_off); B.m2l_cnt = DP<uint32_t>(c->m2l_cnt);
+        B.m2l_list = DP<uint32_t>(c->m2l_list);
+        B.eps2 = c->prm.eps * c->prm.eps;
+        B.nnodes = nn;
+        B.info = DP<int32_t>(c->info);
+        constexpr int W = M2LSmem<MODE, P>::warps;
+        const size_t smem = (size_t)W * M2LSmem<MODE, P>::per_warp;
+        NB_CU(c, cudaFuncSetAttribute(k_m2l<MODE, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_m2l<MODE, P><<<(unsigned)((nn + W - 1) / W), 32 * W, smem, c->st>>>(B);
+        NB_LAUNCHED(c, "m2l");
+        c->launches += 1;
+        for (int r = 1; r <= c->depth; ++r) {
+            const int lo = c->level_start[r], hi = c->level_start[r + 1];
+            if (hi <= lo) continue;
+            k_l2l<MODE, P><<<(unsigned)((hi - lo + 3) / 4), 128, 0, c->st>>>(lo, hi, DP<NodeRec>(c->nodes), box,
+                                                                             DP<H>(c->L));
+            NB_LAUNCHED(c, "l2l");
+            c->launches += 1;
+        }
+    }
+    if (c->timing) cudaEventRecord(c->ev[6], c->st);
 
     const int64_t nl = c->nleaves;
     const int64_t nwork = (uint32_t)c->h_info[INFO_P2P_WORK];
@@ -943,7 +1092,7 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     }
     NB_LAUNCHED(c, "p2p");
     c->launches += npart ? 2 : 1;
-    if (c->timing) cudaEventRecord(c->ev[6], c->st);
+    if (c->timing) cudaEventRecord(c->ev[7], c->st);
     return NBODY_OK;
 }
 

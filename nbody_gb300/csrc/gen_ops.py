@@ -123,6 +123,25 @@ def gen_m2l(p, o):
     o.append("  }")
 
 
+def gen_m2l_v(p, o):
+    """M2L contraction reading the source row M in aligned groups of 4
+    (nb_ld4: one 16-byte load for float, two for double); M must be
+    16-byte aligned and padded to a multiple of 4 entries."""
+    o.append("  template <int ST = 1>")
+    o.append("  static __device__ __forceinline__ void m2l_v(const S* __restrict__ M, const S* D, S* L) {")
+    o.append("    S mq[4];")
+    for n in terms(p):
+        i = idx(n)
+        if i % 4 == 0:
+            o.append(f"    nb_ld4(M + {i}, mq);")
+        dn = sum(n)
+        o.append(f"    {{ const S m = {'-' if dn % 2 else ''}mq[{i % 4}];")
+        for k in terms(p - dn):
+            o.append(f"      L[{idx(k)} * ST] = nb_fma(m, D[{idx(add(n, k))} * ST], L[{idx(k)} * ST]);")
+        o.append("    }")
+    o.append("  }")
+
+
 def gen_mono(p, o, name="mono"):
     o.append(f"  static __device__ __forceinline__ void {name}(S x, S y, S z, S* Y) {{")
     o.append("    Y[0] = S(1);")
@@ -182,6 +201,8 @@ def shift_tables(p):
 def main():
     o = ["// Generated by gen_ops.py -- do not edit.", "#pragma once", ""]
     o.append("template <int P> struct nb_terms { static constexpr int value = (P + 1) * (P + 2) * (P + 3) / 6; };")
+    o.append("// multipole row stride: terms rounded up to a multiple of 4 (16-byte rows for float, 32 for double)")
+    o.append("template <int P> struct nb_tm { static constexpr int value = (nb_terms<P>::value + 3) & ~3; };")
     o.append("template <typename S, int P> struct Ops;")
     for p in range(1, PMAX + 1):
         o.append("")
@@ -189,6 +210,7 @@ def main():
         o.append(f"  static constexpr int T = {T(p)};")
         gen_derivs(p, o)
         gen_m2l(p, o)
+        gen_m2l_v(p, o)
         gen_mono(p, o)
         gen_p2m(p, o)
         gen_l2p(p, o)

@@ -12,7 +12,6 @@
 #define NB_LEVELS 21               // bits per axis of the Morton grid; deepest level
 #define NB_PMAX 8                  // highest expansion order compiled
 #define NB_TMAX 165                // terms at NB_PMAX
-#define NB_WARPS_TRAV 8            // warps per block in the traversal kernel
 
 // error bits raised on the device (ctx->d_info[INFO_ERR])
 #define NB_ERRBIT_PEND_CAP 1u      // refinement list capacity exceeded
@@ -20,7 +19,8 @@
 #define NB_ERRBIT_STACK 4u         // per-warp descent stack overflow
 #define NB_ERRBIT_RANGE 8u         // a particle lay outside a fixed root box
 #define NB_ERRBIT_NONFINITE 16u    // a position was not finite
-#define NB_ERRBIT_M2L_CAP 32u      // recorded far-field list capacity exceeded
+#define NB_ERRBIT_M2L_CAP 32u      // far-field list capacity exceeded
+#define NB_ERRBIT_ASYNC 64u        // an asynchronous copy did not complete within its time limit
 
 // layout of the small device info block (int32 words)
 enum {
@@ -86,7 +86,6 @@ struct nbody_ctx {
     DevBuf M, M32, L, src;
     DevBuf pend_off, pend_cnt, p2p_off, p2p_cnt, pend_list, p2p_list;
     size_t pend_cap = 0, p2p_cap = 0;
-    bool record_m2l = false;       // keep the far-field partner lists (inspection only)
     DevBuf m2l_off, m2l_cnt, m2l_list;
     size_t m2l_cap = 0;
     DevBuf stage;                  // host <-> device staging (interleaved doubles)
@@ -151,6 +150,15 @@ enum { NB_INTEG_NONE = 0, NB_INTEG_KDK_CLOSE = 1, NB_INTEG_EULER = 2 };
 __device__ __forceinline__ float nb_fma(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double nb_fma(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float nb_rsqrt(float s) { return rsqrtf(s); }
+// four consecutive values from a 16-byte aligned address
+__device__ __forceinline__ void nb_ld4(const float* p, float* o) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+__device__ __forceinline__ void nb_ld4(const double* p, double* o) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
 __device__ __forceinline__ double nb_rsqrt(double s) { return rsqrt(s); }
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }

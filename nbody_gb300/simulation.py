@@ -205,9 +205,11 @@ class CudaSimulation:
     def set_timing(self, on: bool = True):
         check(self._h, _lib.load().nbody_set_timing(self._h, int(on)))
 
+    PHASES = ("kick_drift_keys", "sort_gather", "tree", "upward", "lists", "far_field", "near_field")
+
     def phase_times(self):
-        out = np.zeros(6, np.float32)
-        check(self._h, _lib.load().nbody_phase_times(self._h, ptr(out), 6))
+        out = np.zeros(7, np.float32)
+        check(self._h, _lib.load().nbody_phase_times(self._h, ptr(out), 7))
         return out
 
     @property

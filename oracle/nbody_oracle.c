@@ -329,16 +329,21 @@ static void displacement(const orc_ctx* c, int64_t a, int64_t b, double out[3]) 
     for (int d = 0; d < 3; ++d) out[d] = (double)(ca[d] - cb[d]) * u;
 }
 
-/* src/interaction.cl:64-79: approx iff A != B and 3/4 (wA+wB)^2 / d^2 < theta^2 */
+/* src/interaction.cl:64-79 in its own FP32 operation order: approx iff A != B
+   and extent^2 / distance^2 < theta^2 with distance^2 = ((x*x + y*y) + z*z) + 0
+   and extent^2 = (0.75 * (wA+wB)) * (wA+wB), all single precision.  Lengths are
+   in fine units (side / 2^22), a power-of-two rescaling of the reference's box
+   units, which leaves every rounding unchanged.  Compiled without FMA
+   contraction (oracle/Makefile). */
 static int mac_accept(const orc_ctx* c, int64_t t, int64_t s, double theta2) {
     if (t == s) return 0;
     int64_t ct[3], cs[3];
     centre_fine(c, t, ct); centre_fine(c, s, cs);
-    int64_t dx = cs[0] - ct[0], dy = cs[1] - ct[1], dz = cs[2] - ct[2];
-    int64_t d2 = dx * dx + dy * dy + dz * dz;
-    int64_t e = width_fine(c, t) + width_fine(c, s);
-    double lhs = 3.0 * (double)e * (double)e;
-    return lhs < 4.0 * theta2 * (double)d2;
+    float dx = (float)(cs[0] - ct[0]), dy = (float)(cs[1] - ct[1]), dz = (float)(cs[2] - ct[2]);
+    float d2 = ((dx * dx + dy * dy) + dz * dz) + 0.0f;
+    float es = (float)(width_fine(c, t) + width_fine(c, s));
+    float e2 = (0.75f * es) * es;
+    return e2 / d2 < (float)theta2;
 }
 
 /* theta2 is passed as (double)((float)theta * (float)theta), the value the
