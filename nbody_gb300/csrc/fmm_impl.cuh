@@ -280,8 +280,10 @@ __device__ __forceinline__ void centre_fine32(const NodeRec& nd, int& cx, int& c
 
 // MAC of src/interaction.cl:64-79 in its own FP32 operation order: displacement of centres,
 // distance^2 = ((x*x + y*y) + z*z) + w*w with w = 0, extent^2 = (0.75 * (wA+wB)) * (wA+wB),
-// approximate iff extent^2 / distance^2 < theta^2.  Lengths are in fine units, an exact
-// power-of-two rescaling of the reference's box units, so every rounding is the reference's.
+// approximate iff extent^2 / distance^2 < theta^2 (correctly rounded division).  Lengths are in
+// fine units, an exact power-of-two rescaling of the reference's box units, so every rounding is
+// the reference's.  The division is only evaluated when a cheap estimate is within 0.1 % of the
+// threshold, where it could matter; elsewhere the estimate decides the same way.
 __device__ __forceinline__ bool mac_f32(int tcx, int tcy, int tcz, float tw, const NodeRec& s, float theta2) {
     int sx, sy, sz;
     centre_fine32(s, sx, sy, sz);
@@ -289,7 +291,25 @@ __device__ __forceinline__ bool mac_f32(int tcx, int tcy, int tcz, float tw, con
     const float d2 = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)), 0.0f);
     const float es = __fadd_rn(tw, (float)(1u << (NB_LEVELS + 1 - s.level)));
     const float e2 = __fmul_rn(__fmul_rn(0.75f, es), es);
+    const float est = __fdividef(e2, d2);   // within a few ulp of the quotient
+    if (est < 0.999f * theta2) return true;
+    if (est > 1.001f * theta2) return false;
     return __fdiv_rn(e2, d2) < theta2;
+}
+
+// geometry (level, cell coordinates) of the child in octant oct of a node
+struct CellGeom {
+    uint32_t ix, iy, iz;
+    int level;
+};
+__device__ __forceinline__ CellGeom child_geom(const CellGeom& p, int oct) {
+    return CellGeom{2u * p.ix + (oct & 1), 2u * p.iy + ((oct >> 1) & 1), 2u * p.iz + (oct >> 2), p.level + 1};
+}
+__device__ __forceinline__ void geom_centre(const CellGeom& g, int& cx, int& cy, int& cz) {
+    const int sh = NB_LEVELS - g.level;
+    cx = (int)((2u * g.ix + 1u) << sh);
+    cy = (int)((2u * g.iy + 1u) << sh);
+    cz = (int)((2u * g.iz + 1u) << sh);
 }
 
 constexpr int CLS_WARPS = 8;
@@ -727,14 +747,149 @@ __device__ __forceinline__ void p2p_epilogue(const P2PArgs& A, uint32_t i, const
     if (pot) ((R*)A.pot)[i] = -(R)A.G * Ps;
 }
 
-template <int MODE, int P, bool POT>
-__global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p(P2PArgs A) {
+// One warp's share of a near-field work item: every target of the leaf
+// (two per lane, CT lanes per group) against the partner leaves
+// [s_lo, s_hi) of its list.  GUARD: unsoftened kernel, so r = 0 must give 0.
+template <int MODE, int P, bool POT, bool GUARD>
+__device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::S4 (*tile)[P2P_TILE],
+                                         const typename Prec<MODE>::S* sL, uint32_t k, const NodeRec& nt,
+                                         int64_t li, uint32_t chunk, uint32_t nchunk, uint32_t s_lo,
+                                         uint32_t s_hi) {
     typedef typename Prec<MODE>::R R;
+    typedef typename Prec<MODE>::S S;
+    typedef typename Prec<MODE>::S4 S4;
+    constexpr bool KH = Prec<MODE>::kahan;
+    const int lane = lane_id();
+    const double unit = A.box->unit;
+    const S4* src = (const S4*)A.src;
+    const uint32_t cnt_t = nt.count;
+    const int CT = cnt_t <= 16 ? 8 : cnt_t <= 32 ? 16 : 32;
+    const int NG = 32 / CT, grp = lane / CT, gl = lane % CT, TPL = P2P_TILE / CT;
+    const uint32_t loff = A.p2p_off[k];
+    const S eps2 = (S)A.eps2;
+    S4 zero4;
+    zero4.x = 0; zero4.y = 0; zero4.z = 0; zero4.w = 0;
+    for (uint32_t tc = 0; tc < cnt_t; tc += 2 * CT) {
+        const uint32_t ta = tc + gl, tb = tc + CT + gl;
+        const bool va = ta < cnt_t, vb = tb < cnt_t;
+        const uint32_t ia = nt.begin + (va ? ta : 0), ib = nt.begin + (vb ? tb : 0);
+        const S4 ya = src[ia], yb = src[ib];
+        S ax = 0, ay = 0, az = 0, ap = 0, bx = 0, by = 0, bz = 0, bp = 0;
+        S cax = 0, cay = 0, caz = 0, cap = 0, cbx = 0, cby = 0, cbz = 0, cbp = 0;
+        for (uint32_t base = s_lo; base < s_hi; base += 32) {
+            const uint32_t nb = min(32u, s_hi - base);
+            uint32_t my_s = 0, my_beg = 0, my_cnt = 0;
+            S my_dx = 0, my_dy = 0, my_dz = 0;
+            if ((uint32_t)lane < nb) {
+                my_s = A.p2p_list[loff + base + lane];
+                const NodeRec sn = A.nodes[my_s];
+                my_beg = sn.begin;
+                my_cnt = sn.count;
+                double ddx, ddy, ddz;
+                disp(sn, nt, unit, ddx, ddy, ddz);
+                my_dx = (S)ddx; my_dy = (S)ddy; my_dz = (S)ddz;
+            }
+            const uint32_t rounds = (nb + NG - 1) / NG;
+            uint32_t rr = 0, sb = 0;
+            const uint32_t cur_beg = __shfl_sync(0xffffffffu, my_beg, grp);
+            const uint32_t cur_cnt0 = __shfl_sync(0xffffffffu, my_cnt, grp);
+            const uint32_t cur_cnt = (uint32_t)grp < nb ? cur_cnt0 : 0u;
+            S4 pre[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const uint32_t j = sb + gl + e * CT;
+                pre[e] = (e < TPL && j < cur_cnt) ? src[cur_beg + j] : zero4;
+            }
+            while (rr < rounds) {
+                const uint32_t q = rr * NG + grp;
+                const uint32_t qs = q & 31;
+                const uint32_t s_id = __shfl_sync(0xffffffffu, my_s, qs);
+                const S dx = __shfl_sync(0xffffffffu, my_dx, qs), dy = __shfl_sync(0xffffffffu, my_dy, qs),
+                        dz = __shfl_sync(0xffffffffu, my_dz, qs);
+                const uint32_t scnt0 = __shfl_sync(0xffffffffu, my_cnt, qs);
+                const uint32_t scnt = q < nb ? scnt0 : 0u;
+                uint32_t mx = scnt;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (e < TPL) tile[grp][gl + e * CT] = pre[e];
+                __syncwarp();
+                uint32_t nrr = rr, nsb = sb + P2P_TILE;
+                if (nsb >= mx) { nrr = rr + 1; nsb = 0; }
+                {
+                    const uint32_t nq = nrr * NG + grp;
+                    const uint32_t nbeg = __shfl_sync(0xffffffffu, my_beg, nq & 31);
+                    const uint32_t ncnt0 = __shfl_sync(0xffffffffu, my_cnt, nq & 31);
+                    const uint32_t ncnt = (nrr < rounds && nq < nb) ? ncnt0 : 0u;
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const uint32_t j = nsb + gl + e * CT;
+                        pre[e] = (e < TPL && j < ncnt) ? src[nbeg + j] : zero4;
+                    }
+                }
+                // both targets, shifted into the source leaf's frame
+                const S xa = ya.x - dx, ya_ = ya.y - dy, za = ya.z - dz;
+                const S xb = yb.x - dx, yb_ = yb.y - dy, zb = yb.z - dz;
+                const int nj = scnt > sb ? min((int)(scnt - sb), P2P_TILE) : 0;
+                S pax = 0, pay = 0, paz = 0, pap = 0, pbx = 0, pby = 0, pbz = 0, pbp = 0;
+#pragma unroll 2
+                for (int e = 0; e < nj; ++e) {
+                    const S4 sj = tile[grp][e];
+                    const S rxa = sj.x - xa, rya = sj.y - ya_, rza = sj.z - za;
+                    const S rxb = sj.x - xb, ryb = sj.y - yb_, rzb = sj.z - zb;
+                    S s2a = nb_fma(rxa, rxa, nb_fma(rya, rya, nb_fma(rza, rza, eps2)));
+                    S s2b = nb_fma(rxb, rxb, nb_fma(ryb, ryb, nb_fma(rzb, rzb, eps2)));
+                    if (GUARD) { s2a = s2a > S(0) ? s2a : S(1e30); s2b = s2b > S(0) ? s2b : S(1e30); }
+                    S inva = nb_rsqrt(s2a), invb = nb_rsqrt(s2b);
+                    if (POT && s_id == k && sb + e == ta) inva = S(0);
+                    if (POT && s_id == k && sb + e == tb) invb = S(0);
+                    const S wa = sj.w * inva * inva * inva, wb = sj.w * invb * invb * invb;
+                    pax = nb_fma(rxa, wa, pax); pay = nb_fma(rya, wa, pay); paz = nb_fma(rza, wa, paz);
+                    pbx = nb_fma(rxb, wb, pbx); pby = nb_fma(ryb, wb, pby); pbz = nb_fma(rzb, wb, pbz);
+                    if (POT) { pap = nb_fma(sj.w, inva, pap); pbp = nb_fma(sj.w, invb, pbp); }
+                }
+                if (KH) {
+                    kahan_add(ax, cax, pax); kahan_add(ay, cay, pay); kahan_add(az, caz, paz);
+                    kahan_add(bx, cbx, pbx); kahan_add(by, cby, pby); kahan_add(bz, cbz, pbz);
+                    if (POT) { kahan_add(ap, cap, pap); kahan_add(bp, cbp, pbp); }
+                } else {
+                    ax += pax; ay += pay; az += paz; bx += pbx; by += pby; bz += pbz;
+                    if (POT) { ap += pap; bp += pbp; }
+                }
+                __syncwarp();
+                rr = nrr;
+                sb = nsb;
+            }
+        }
+        // combine the source groups in a fixed order, in the state precision
+        R Ax = (R)ax - (R)cax, Ay = (R)ay - (R)cay, Az = (R)az - (R)caz, Ap = (R)ap - (R)cap;
+        R Bx = (R)bx - (R)cbx, By = (R)by - (R)cby, Bz = (R)bz - (R)cbz, Bp = (R)bp - (R)cbp;
+        for (int o = CT; o < 32; o <<= 1) {
+            Ax += shfl_xor_t(Ax, o); Ay += shfl_xor_t(Ay, o); Az += shfl_xor_t(Az, o);
+            Bx += shfl_xor_t(Bx, o); By += shfl_xor_t(By, o); Bz += shfl_xor_t(Bz, o);
+            if (POT) { Ap += shfl_xor_t(Ap, o); Bp += shfl_xor_t(Bp, o); }
+        }
+        if (grp == 0) {
+            if (nchunk == 1) {
+                if (va) p2p_epilogue<MODE, P>(A, ia, sL, ya, Ax, Ay, Az, Ap, POT);
+                if (vb) p2p_epilogue<MODE, P>(A, ib, sL, yb, Bx, By, Bz, Bp, POT);
+            } else {
+                R* pt = (R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)chunk * cnt_t);
+                if (va) { pt[4 * ta] = Ax; pt[4 * ta + 1] = Ay; pt[4 * ta + 2] = Az; pt[4 * ta + 3] = Ap; }
+                if (vb) { pt[4 * tb] = Bx; pt[4 * tb + 1] = By; pt[4 * tb + 2] = Bz; pt[4 * tb + 3] = Bp; }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <int MODE, int P, bool POT>
+__global__ void __launch_bounds__(32 * P2P_WARPS, 5) k_p2p(P2PArgs A) {
     typedef typename Prec<MODE>::S S;
     typedef typename Prec<MODE>::H H;
     typedef typename Prec<MODE>::S4 S4;
     constexpr int T = nb_terms<P>::value;
-    constexpr bool KH = Prec<MODE>::kahan;
     __shared__ S4 tile[P2P_WARPS][4][P2P_TILE];
     __shared__ S sL[P2P_WARPS][T];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
@@ -751,130 +906,15 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p(P2PArgs A) {
     const uint32_t nchunk = A.work_off[li + 1] - A.work_off[li];
     const uint32_t k = A.leaves[li];
     const NodeRec nt = A.nodes[k];
-    const double unit = A.box->unit;
-    const S4* src = (const S4*)A.src;
     if (nchunk == 1) {
         const H* Lg = (const H*)A.L;
         for (int a = lane; a < T; a += 32) sL[wib][a] = (S)Lg[(int64_t)k * T + a];
     }
-    const uint32_t cnt_t = nt.count;
-    // lanes per target group (8, 16 or 32); NG = 32 / CT <= 4 source groups, one tile each
-    const int CT = cnt_t <= 8 ? 8 : cnt_t <= 16 ? 16 : 32;
-    const int NG = 32 / CT, grp = lane / CT, gl = lane % CT, TPL = P2P_TILE / CT;
-    const uint32_t loff = A.p2p_off[k], lcnt = A.p2p_cnt[k];
+    const uint32_t lcnt = A.p2p_cnt[k];
     const uint32_t s_lo = chunk * P2P_CHUNK, s_hi = min(lcnt, s_lo + P2P_CHUNK);
-    const S eps2 = (S)A.eps2;
-    S4 zero4;
-    zero4.x = 0; zero4.y = 0; zero4.z = 0; zero4.w = 0;
     __syncwarp();
-    for (uint32_t tc = 0; tc < cnt_t; tc += CT) {
-        const uint32_t ti = tc + gl;
-        const bool tvalid = ti < cnt_t;
-        const uint32_t i = nt.begin + (tvalid ? ti : 0);
-        const S4 yi = src[i];
-        S ex = 0, ey = 0, ez = 0, ps = 0, cx = 0, cy = 0, cz = 0, cp = 0;
-        for (uint32_t base = s_lo; base < s_hi; base += 32) {
-            const uint32_t nb = min(32u, s_hi - base);
-            // partner records, one per lane
-            uint32_t my_s = 0, my_beg = 0, my_cnt = 0;
-            S my_dx = 0, my_dy = 0, my_dz = 0;
-            if ((uint32_t)lane < nb) {
-                my_s = A.p2p_list[loff + base + lane];
-                const NodeRec sn = A.nodes[my_s];
-                my_beg = sn.begin;
-                my_cnt = sn.count;
-                double ddx, ddy, ddz;
-                disp(sn, nt, unit, ddx, ddy, ddz);
-                my_dx = (S)ddx; my_dy = (S)ddy; my_dz = (S)ddz;
-            }
-            const uint32_t rounds = (nb + NG - 1) / NG;
-            // the sequence of steps: (round rr, sub-tile sb); fetch the first
-            uint32_t rr = 0, sb = 0;
-            const uint32_t cur_beg = __shfl_sync(0xffffffffu, my_beg, grp);
-            const uint32_t cur_cnt0 = __shfl_sync(0xffffffffu, my_cnt, grp);
-            const uint32_t cur_cnt = (uint32_t)grp < nb ? cur_cnt0 : 0u;
-            S4 pre[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const uint32_t j = sb + gl + e * CT;
-                pre[e] = (e < TPL && j < cur_cnt) ? src[cur_beg + j] : zero4;
-            }
-            while (rr < rounds) {
-                // current step's geometry
-                const uint32_t q = rr * NG + grp;
-                const uint32_t qs = q & 31;
-                const uint32_t s_id = __shfl_sync(0xffffffffu, my_s, qs);
-                const S dx = __shfl_sync(0xffffffffu, my_dx, qs), dy = __shfl_sync(0xffffffffu, my_dy, qs),
-                        dz = __shfl_sync(0xffffffffu, my_dz, qs);
-                const uint32_t scnt0 = __shfl_sync(0xffffffffu, my_cnt, qs);
-                const uint32_t scnt = q < nb ? scnt0 : 0u;
-                uint32_t mx = scnt;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-                // store the prefetched tile
-#pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    if (e < TPL) tile[wib][grp][gl + e * CT] = pre[e];
-                __syncwarp();
-                // next step and its prefetch
-                uint32_t nrr = rr, nsb = sb + P2P_TILE;
-                if (nsb >= mx) { nrr = rr + 1; nsb = 0; }
-                {
-                    const uint32_t nq = nrr * NG + grp;
-                    const uint32_t nbeg = __shfl_sync(0xffffffffu, my_beg, nq & 31);
-                    const uint32_t ncnt0 = __shfl_sync(0xffffffffu, my_cnt, nq & 31);
-                    const uint32_t ncnt = (nrr < rounds && nq < nb) ? ncnt0 : 0u;
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const uint32_t j = nsb + gl + e * CT;
-                        pre[e] = (e < TPL && j < ncnt) ? src[nbeg + j] : zero4;
-                    }
-                }
-                // evaluate the current tile against this lane's target, shifted into the source leaf's frame
-                const S yx = yi.x - dx, yy = yi.y - dy, yz = yi.z - dz;
-                const int nj = scnt > sb ? min((int)(scnt - sb), P2P_TILE) : 0;
-                S px = 0, py = 0, pz = 0, pp = 0;
-#pragma unroll 4
-                for (int e = 0; e < nj; ++e) {
-                    const S4 sj = tile[wib][grp][e];
-                    const S rx = sj.x - yx, ry = sj.y - yy, rz = sj.z - yz;
-                    const S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
-                    S inv = s2 > S(0) ? nb_rsqrt(s2) : S(0);
-                    if (POT && s_id == k && sb + e == ti) inv = S(0);
-                    const S w3 = sj.w * inv * inv * inv;
-                    px = nb_fma(rx, w3, px);
-                    py = nb_fma(ry, w3, py);
-                    pz = nb_fma(rz, w3, pz);
-                    if (POT) pp = nb_fma(sj.w, inv, pp);
-                }
-                if (KH) {
-                    kahan_add(ex, cx, px); kahan_add(ey, cy, py); kahan_add(ez, cz, pz);
-                    if (POT) kahan_add(ps, cp, pp);
-                } else {
-                    ex += px; ey += py; ez += pz;
-                    if (POT) ps += pp;
-                }
-                __syncwarp();
-                rr = nrr;
-                sb = nsb;
-            }
-        }
-        // combine the source groups in a fixed order, in the state precision
-        R Ex = (R)ex - (R)cx, Ey = (R)ey - (R)cy, Ez = (R)ez - (R)cz, Ps = (R)ps - (R)cp;
-        for (int o = CT; o < 32; o <<= 1) {
-            Ex += shfl_xor_t(Ex, o); Ey += shfl_xor_t(Ey, o); Ez += shfl_xor_t(Ez, o);
-            if (POT) Ps += shfl_xor_t(Ps, o);
-        }
-        if (grp == 0 && tvalid) {
-            if (nchunk == 1) {
-                p2p_epilogue<MODE, P>(A, i, sL[wib], yi, Ex, Ey, Ez, Ps, POT);
-            } else {
-                R* pt = (R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)chunk * cnt_t + ti);
-                pt[0] = Ex; pt[1] = Ey; pt[2] = Ez; pt[3] = Ps;
-            }
-        }
-        __syncwarp();
-    }
+    if (A.eps2 > 0.0) p2p_item<MODE, P, POT, false>(A, tile[wib], sL[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
+    else p2p_item<MODE, P, POT, true>(A, tile[wib], sL[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
 }
 
 // sums the chunk partials of multi-chunk leaves in chunk order, then L2P + epilogue

@@ -44,7 +44,8 @@ struct __align__(16) NodeRec {
     int32_t parent;                // -1 for the root
     int32_t child_begin;           // first child (children are contiguous)
     uint8_t level, nchild;         // nchild == 0 <=> leaf
-    uint16_t pad;
+    uint8_t child_mask;            // bit k set <=> the child in octant k exists (children stored in octant order)
+    uint8_t pad;
 };
 static_assert(sizeof(NodeRec) == 32, "NodeRec must stay 32 bytes");
 

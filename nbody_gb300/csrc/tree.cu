@@ -246,6 +246,7 @@ __global__ void __launch_bounds__(TB) k_tree_nodes(int64_t nnodes, int64_t n, in
     nd.level = (uint8_t)l;
     nd.begin = b;
     nd.pad = 0;
+    nd.child_mask = 0;
     if (l == 0) {
         nd.count = (uint32_t)n;
         nd.ix = nd.iy = nd.iz = 0;
@@ -270,6 +271,10 @@ __global__ void __launch_bounds__(TB) k_tree_nodes(int64_t nnodes, int64_t n, in
         if (hi > lo) {
             nd.child_begin = (int32_t)lo;
             nd.nchild = (uint8_t)(hi - lo);
+            const int csh = 3 * (NB_LEVELS - l - 1);
+            uint32_t mask = 0;
+            for (int64_t c = lo; c < hi; ++c) mask |= 1u << ((keys[sv[c]] >> csh) & 7u);
+            nd.child_mask = (uint8_t)mask;
         }
     }
     nodes[k] = nd;
