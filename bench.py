@@ -24,6 +24,7 @@ Under torchrun each rank runs an independent replica on its own GPU.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -186,6 +187,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-targets", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--adj-steps", type=int, default=10, help="steps of the timed forward+adjoint run (0: skip)")
+    ap.add_argument("--adj-every", type=int, default=2, help="checkpoint spacing of the forward+adjoint run")
     a = ap.parse_args()
     assert a.warmup >= 0 and a.steps >= 1
     rank, world, local = dist_env()
@@ -269,6 +272,46 @@ def main():
         e2e_s = float(t.item())
     e2e = a.n * a.e2e_steps * world / e2e_s
 
+    # forward + adjoint: a recorded run of adj_steps steps and its reverse sweep, with the loss
+    # L = sum(wx . x_N + wv . v_N); seeds and gradients stay on the device
+    fwd_adj = None
+    if a.adj_steps > 0:
+        dev = torch.device("cuda", local)
+        g = torch.Generator(device=dev).manual_seed(7)
+        wx = torch.randn((a.n, 3), dtype=torch.float64, device=dev, generator=g)
+        wv = torch.randn((a.n, 3), dtype=torch.float64, device=dev, generator=g)
+        out = [torch.empty((a.n, 3), dtype=torch.float64, device=dev) for _ in range(2)] + \
+              [torch.empty(a.n, dtype=torch.float64, device=dev) for _ in range(2)]
+        dp = lambda t: ctypes.c_void_p(t.data_ptr())
+        L = _lib.load()
+
+        def fwd_bwd(k):
+            _lib.check(sim._h, L.nbody_forward_checkpointed(sim._h, k, a.adj_every, None))
+            _lib.check(sim._h, L.nbody_backward(sim._h, dp(wx), dp(wv), *(dp(t) for t in out)))
+
+        fwd_bwd(min(2, a.adj_steps))           # warm-up: snapshot and adjoint buffers
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ea.record(stream)
+        fwd_bwd(a.adj_steps)
+        eb.record(stream)
+        torch.cuda.synchronize()
+        adj_ms = ea.elapsed_time(eb)
+        if world > 1:
+            t = torch.tensor([adj_ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            adj_ms = float(t.item())
+        fin = all(bool(torch.isfinite(t).all()) for t in out)
+        fwd_adj = {"value": a.n * a.adj_steps * world / (adj_ms * 1e-3), "unit": UNIT,
+                   "ms_per_step": adj_ms / a.adj_steps, "steps": a.adj_steps, "checkpoint_every": a.adj_every,
+                   "gradients_finite": fin,
+                   "note": "one recorded leapfrog run of `steps` steps plus its reverse sweep (frozen-tree "
+                           "discrete adjoint: one force VJP per time point, re-evaluation from snapshots); "
+                           "loss sum(wx . x_N + wv . v_N), seeds and gradients resident on the device"}
+        del out, wx, wv
+
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -306,7 +349,7 @@ def main():
         "dtype": "f32+f64" if a.precision == "mixed" else ("f32" if a.precision == "fp32" else "f64"),
         "data": f"synthetic seeded collision ICs (seed {a.seed} + rank)", "config": workload_desc(a),
         "rms_force_err_vs_fp64_direct": rms_err, "max_force_err_vs_fp64_direct": max_err,
-        "err_targets": int(len(tg)), "fwd_adjoint": None,
+        "err_targets": int(len(tg)), "fwd_adjoint": fwd_adj,
         "phase_ms_per_step": {k: float(v) for k, v in zip(nb.CudaSimulation.PHASES, per_step)},
         "work_per_step": stats, "wall_s_timed": wall,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": a.n * 8 * 11, "d2h_bytes_per_step": a.n * 8 * 9,

@@ -101,6 +101,36 @@ int nbody_step(nbody_ctx* c, int nsteps, double* t_out);
    (computeForceBuffers, src/open_cl_simulation.cpp:486-570). */
 int nbody_compute_forces(nbody_ctx* c, double* acc, double* pot);
 
+/* Adjoint (no counterpart in the reference, which has no gradients).
+   Arrays are in input order; pointers may be host or device memory; any
+   output may be NULL.  Derivatives are those of the FMM forces with the tree
+   and interaction lists of each evaluation held fixed (the lists change only
+   where a particle crosses a cell boundary or a cell pair crosses the
+   acceptance threshold, where the force itself jumps).
+
+   nbody_force_vjp: one force evaluation at the current positions and, for
+   S = sum_i mu_i . a_i with mu (n x 3), gx = dS/dx (n x 3), gq = dS/dq (n),
+   gm = dS/dm (n).  A zero-charge particle's gq omits the term
+   G/m_i mu_i . E_i (its acceleration does not carry E_i). */
+int nbody_force_vjp(nbody_ctx* c, const double* mu, double* gx, double* gq, double* gm);
+
+/* Advances nsteps leapfrog (KDK) steps like nbody_step, recording the sorted
+   state every `every` steps (plus the final state) for nbody_backward.  Device
+   memory: (ceil(nsteps / every) + every) snapshots of about 92 bytes per
+   particle in the FP64 and mixed forms, 48 in FP32.  every = 1 or 2 costs one
+   extra force evaluation per step in the reverse sweep; larger spacings
+   recompute the steps in between (about (2 every - 2) / every evaluations per
+   step). */
+int nbody_forward_checkpointed(nbody_ctx* c, int nsteps, int every, double* t_out);
+
+/* Reverse sweep of the run recorded by the last nbody_forward_checkpointed:
+   given gxT = dL/dx_N and gvT = dL/dv_N (n x 3 each; NULL = zero), returns
+   gx0 = dL/dx_0, gv0 = dL/dv_0 (n x 3), gq = dL/dq and gm = dL/dm (n).  The
+   context's state is that run's final state again on return.  The recording
+   is dropped by nbody_set_state and nbody_step. */
+int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* gx0, double* gv0, double* gq,
+                   double* gm);
+
 /* FP64 diagnostics of the current state: out[0] kinetic energy, out[1]
    potential energy, out[2..4] momentum, out[5..7] angular momentum,
    out[8] total mass.  (The reference computes none.) */

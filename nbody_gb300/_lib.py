@@ -25,7 +25,8 @@ EXPORTS = ("nbody_default_params", "nbody_create", "nbody_destroy", "nbody_set_s
            "nbody_step", "nbody_compute_forces", "nbody_diagnostics", "nbody_tree_info", "nbody_get_tree",
            "nbody_get_interactions", "nbody_set_timing", "nbody_phase_times", "nbody_stream", "nbody_get_time",
            "nbody_last_error", "nbody_direct_forces", "nbody_get_stats", "nbody_flops_per_m2l", "nbody_flops_per_p2p",
-           "nbody_measure_peaks", "nbody_direct_forces_static")
+           "nbody_measure_peaks", "nbody_direct_forces_static", "nbody_force_vjp", "nbody_forward_checkpointed",
+           "nbody_backward")
 
 
 class Params(C.Structure):
@@ -72,6 +73,9 @@ def load(path: str | None = None):
     L.nbody_direct_forces_static.argtypes = [C.c_int, C.c_int64, vp, vp, vp, C.c_double, C.c_double, C.c_int64, vp,
                                              vp, vp, vp]
     L.nbody_step.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
+    L.nbody_force_vjp.argtypes = [vp, vp, vp, vp, vp]
+    L.nbody_forward_checkpointed.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.nbody_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.nbody_compute_forces.argtypes = [vp, vp, vp]
     L.nbody_diagnostics.argtypes = [vp, vp]
     L.nbody_tree_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),

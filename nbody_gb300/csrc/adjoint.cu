@@ -1,0 +1,246 @@
+// C ABI of the adjoint: one force vector-Jacobian product, a leapfrog run that
+// records sorted-state snapshots, and the reverse sweep over that run.
+// Declarations are in include/nbody_gb300.h.
+//
+// Reverse sweep of N kick-drift-kick steps (time points 0..N):
+//   lambda_v is continuous through the kicks, lambda_x through the drifts;
+//   at time point pt the force a(x_pt) entered the kicks with weight
+//   c = dt/2 (pt = 0 or N) or dt (both half kicks of an interior point), so
+//   its VJP is taken with mu = c lambda_v and added to lambda_x, q and m;
+//   before time point pt < N the drift x_{pt+1} = x_pt + dt v gives
+//   lambda_v += dt lambda_x.
+// Forces at a time point need its tree, lists and local expansions, so each
+// time point is re-evaluated from a snapshot (the run's last point and the last
+// point of every recomputed segment are already current).  Snapshots hold the
+// sorted state (positions, velocities, accelerations, masses, charges, ids), so
+// a recomputed segment is bitwise the recorded one.
+#include <algorithm>
+
+#include "nbody_internal.cuh"
+
+namespace {
+
+constexpr int TB = 256;
+inline unsigned nblk(int64_t n) { return (unsigned)((n + TB - 1) / TB); }
+
+template <typename R>
+__global__ void k_to_r(int64_t n, const double* __restrict__ a, R* __restrict__ o) {
+    const int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x;
+    if (i < n) o[i] = (R)a[i];
+}
+
+template <typename R>
+__global__ void k_to_d(int64_t n, const R* __restrict__ a, double* __restrict__ o) {
+    const int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x;
+    if (i < n) o[i] = (double)a[i];
+}
+
+// reverse drift: lambda_v += dt lambda_x
+template <typename R>
+__global__ void k_rev_drift(int64_t n, R* __restrict__ lv, const R* __restrict__ lx, double dt) {
+    const int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x;
+    if (i < n) lv[i] += (R)dt * lx[i];
+}
+
+// snapshot layout: 11 state arrays of n scalars (x y z vx vy vz ax ay az m q) then n ids
+size_t snapshot_bytes(const nbody_ctx* c) {
+    const size_t b = (11 * c->rsz + sizeof(uint32_t)) * (size_t)c->n;
+    return (b + 255) / 256 * 256;
+}
+
+DevBuf* state_arrays(nbody_ctx* c, int k, DevBuf** out) {
+    DevBuf* a[11] = {&c->x[k], &c->y[k], &c->z[k], &c->vx[k], &c->vy[k], &c->vz[k],
+                     &c->ax[k], &c->ay[k], &c->az[k], &c->m[k], &c->q[k]};
+    for (int i = 0; i < 11; ++i) out[i] = a[i];
+    return &c->id[k];
+}
+
+int snap_save(nbody_ctx* c, int slot) {
+    unsigned char* base = (unsigned char*)c->snaps.p + (size_t)slot * c->snap_bytes;
+    const size_t rb = c->rsz * (size_t)c->n;
+    DevBuf* arr[11];
+    DevBuf* id = state_arrays(c, c->cur, arr);
+    for (int i = 0; i < 11; ++i)
+        NB_CU(c, cudaMemcpyAsync(base + i * rb, arr[i]->p, rb, cudaMemcpyDeviceToDevice, c->st));
+    NB_CU(c, cudaMemcpyAsync(base + 11 * rb, id->p, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToDevice, c->st));
+    return NBODY_OK;
+}
+
+int snap_load(nbody_ctx* c, int slot) {
+    const unsigned char* base = (const unsigned char*)c->snaps.p + (size_t)slot * c->snap_bytes;
+    const size_t rb = c->rsz * (size_t)c->n;
+    DevBuf* arr[11];
+    DevBuf* id = state_arrays(c, c->cur, arr);
+    for (int i = 0; i < 11; ++i)
+        NB_CU(c, cudaMemcpyAsync(arr[i]->p, base + i * rb, rb, cudaMemcpyDeviceToDevice, c->st));
+    NB_CU(c, cudaMemcpyAsync(id->p, base + 11 * rb, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToDevice, c->st));
+    c->have_acc = true;
+    return NBODY_OK;
+}
+
+int vjp(nbody_ctx* c, double coef) {
+    switch (c->prm.precision) {
+        case NBODY_PREC_FP32: return nb_fmm_vjp_fp32(c, coef);
+        case NBODY_PREC_MIXED: return nb_fmm_vjp_mixed(c, coef);
+        default: return nb_fmm_vjp_fp64(c, coef);
+    }
+}
+
+int alloc_adjoint(nbody_ctx* c) {
+    const size_t rb = c->rsz * (size_t)c->n;
+    NB_TRY(nb_grow(c, c->adj_lx, 3 * rb));
+    NB_TRY(nb_grow(c, c->adj_lv, 3 * rb));
+    NB_TRY(nb_grow(c, c->adj_gq, rb));
+    NB_TRY(nb_grow(c, c->adj_gm, rb));
+    return NBODY_OK;
+}
+
+// host or device double array -> R buffer (through the staging area)
+int upload_r(nbody_ctx* c, const double* src, int64_t cnt, DevBuf& dst, double* stage) {
+    if (src) {
+        NB_CU(c, cudaMemcpyAsync(stage, src, sizeof(double) * cnt, cudaMemcpyDefault, c->st));
+        if (c->rsz == 4) k_to_r<float><<<nblk(cnt), TB, 0, c->st>>>(cnt, stage, DP<float>(dst));
+        else k_to_r<double><<<nblk(cnt), TB, 0, c->st>>>(cnt, stage, DP<double>(dst));
+        NB_LAUNCHED(c, "adjoint upload");
+    } else {
+        NB_CU(c, cudaMemsetAsync(dst.p, 0, c->rsz * cnt, c->st));
+    }
+    return NBODY_OK;
+}
+
+int download_r(nbody_ctx* c, const DevBuf& src, int64_t cnt, double* dst, double* stage) {
+    if (!dst) return NBODY_OK;
+    if (c->rsz == 4) k_to_d<float><<<nblk(cnt), TB, 0, c->st>>>(cnt, DP<float>(src), stage);
+    else k_to_d<double><<<nblk(cnt), TB, 0, c->st>>>(cnt, DP<double>(src), stage);
+    NB_LAUNCHED(c, "adjoint download");
+    NB_CU(c, cudaMemcpyAsync(dst, stage, sizeof(double) * cnt, cudaMemcpyDefault, c->st));
+    return NBODY_OK;
+}
+
+int rev_drift(nbody_ctx* c) {
+    const int64_t n3 = 3 * c->n;
+    if (c->rsz == 4) k_rev_drift<float><<<nblk(n3), TB, 0, c->st>>>(n3, DP<float>(c->adj_lv), DP<float>(c->adj_lx),
+                                                                      c->prm.dt);
+    else k_rev_drift<double><<<nblk(n3), TB, 0, c->st>>>(n3, DP<double>(c->adj_lv), DP<double>(c->adj_lx),
+                                                           c->prm.dt);
+    NB_LAUNCHED(c, "reverse drift");
+    return NBODY_OK;
+}
+
+// snapshot slots: 0 .. nck-1 checkpoints, then `every - 1` segment slots, then the final state
+int nck(const nbody_ctx* c) { return (c->ck_steps + c->ck_every - 1) / c->ck_every; }
+int seg_slot(const nbody_ctx* c, int j) { return nck(c) + j; }
+int final_slot(const nbody_ctx* c) { return nck(c) + c->ck_every - 1; }
+
+}  // namespace
+
+extern "C" {
+
+int nbody_force_vjp(nbody_ctx* c, const double* mu, double* gx, double* gq, double* gm) {
+    if (!c || !mu) return NBODY_ERR_INVALID;
+    if (c->n == 0) return nb_fail(c, NBODY_ERR_STATE, "no particles");
+    NB_CU(c, cudaSetDevice(c->device));
+    const int64_t n = c->n;
+    NB_TRY(alloc_adjoint(c));
+    NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
+    c->have_acc = c->prm.integrator == NBODY_INTEG_LEAPFROG;
+    double* st = DP<double>(c->stage);
+    NB_TRY(upload_r(c, mu, 3 * n, c->adj_lv, st));
+    NB_CU(c, cudaMemsetAsync(c->adj_lx.p, 0, 3 * c->rsz * n, c->st));
+    NB_CU(c, cudaMemsetAsync(c->adj_gq.p, 0, c->rsz * n, c->st));
+    NB_CU(c, cudaMemsetAsync(c->adj_gm.p, 0, c->rsz * n, c->st));
+    const int64_t l0 = c->launches;
+    NB_TRY(vjp(c, 1.0));
+    NB_TRY(download_r(c, c->adj_lx, 3 * n, gx, st));
+    NB_TRY(download_r(c, c->adj_gq, n, gq, st + 3 * n));
+    NB_TRY(download_r(c, c->adj_gm, n, gm, st + 4 * n));
+    NB_CU(c, cudaStreamSynchronize(c->st));
+    c->launches = c->launches - l0;
+    return NBODY_OK;
+}
+
+int nbody_forward_checkpointed(nbody_ctx* c, int nsteps, int every, double* t_out) {
+    if (!c) return NBODY_ERR_INVALID;
+    if (c->n == 0) return nb_fail(c, NBODY_ERR_STATE, "no particles");
+    if (c->prm.integrator != NBODY_INTEG_LEAPFROG)
+        return nb_fail(c, NBODY_ERR_INVALID, "the recorded run needs the leapfrog integrator");
+    if (nsteps < 1 || every < 1) return nb_fail(c, NBODY_ERR_INVALID, "nsteps and every must be >= 1");
+    NB_CU(c, cudaSetDevice(c->device));
+    every = std::min(every, nsteps);
+    c->ck_steps = 0;
+    c->snap_bytes = snapshot_bytes(c);
+    const int slots = (nsteps + every - 1) / every + every;
+    NB_TRY(nb_grow(c, c->snaps, c->snap_bytes * (size_t)slots));
+    if (!c->have_acc) {
+        NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
+        c->have_acc = true;
+    }
+    c->ck_t0 = c->time;
+    c->ck_every = every;
+    c->ck_steps = nsteps;
+    NB_TRY(snap_save(c, 0));
+    for (int s = 0; s < nsteps; ++s) {
+        NB_TRY(nb_evaluate(c, 1, NB_INTEG_KDK_CLOSE, false));
+        c->time += c->prm.dt;
+        const int pt = s + 1;
+        if (pt < nsteps && pt % every == 0) NB_TRY(snap_save(c, pt / every));
+    }
+    NB_TRY(snap_save(c, final_slot(c)));
+    NB_CU(c, cudaStreamSynchronize(c->st));
+    c->tree_at_final = true;
+    if (t_out) *t_out = c->time;
+    return NBODY_OK;
+}
+
+int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* gx0, double* gv0, double* gq,
+                   double* gm) {
+    if (!c) return NBODY_ERR_INVALID;
+    if (c->ck_steps < 1) return nb_fail(c, NBODY_ERR_STATE, "no recorded run (call nbody_forward_checkpointed)");
+    NB_CU(c, cudaSetDevice(c->device));
+    const int64_t n = c->n;
+    const int N = c->ck_steps, every = c->ck_every;
+    const double dt = c->prm.dt;
+    NB_TRY(alloc_adjoint(c));
+    double* st = DP<double>(c->stage);
+    NB_TRY(upload_r(c, gxT, 3 * n, c->adj_lx, st));
+    NB_TRY(upload_r(c, gvT, 3 * n, c->adj_lv, st + 3 * n));
+    NB_CU(c, cudaMemsetAsync(c->adj_gq.p, 0, c->rsz * n, c->st));
+    NB_CU(c, cudaMemsetAsync(c->adj_gm.p, 0, c->rsz * n, c->st));
+    // time point N
+    if (!c->tree_at_final) {
+        NB_TRY(snap_load(c, final_slot(c)));
+        NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
+    }
+    NB_TRY(vjp(c, 0.5 * dt));
+    // segments [s0, e), last first
+    for (int s0 = ((N - 1) / every) * every; s0 >= 0; s0 -= every) {
+        const int e = std::min(s0 + every, N);
+        NB_TRY(snap_load(c, s0 / every));
+        c->time = c->ck_t0 + s0 * dt;
+        for (int pt = s0 + 1; pt <= e - 1; ++pt) {       // recompute x_{s0+1} .. x_{e-1}
+            NB_TRY(nb_evaluate(c, 1, NB_INTEG_KDK_CLOSE, false));
+            if (pt < e - 1) NB_TRY(snap_save(c, seg_slot(c, pt - s0 - 1)));
+        }
+        for (int pt = e - 1; pt >= s0; --pt) {
+            NB_TRY(rev_drift(c));
+            if (pt < e - 1) {
+                NB_TRY(snap_load(c, pt == s0 ? s0 / every : seg_slot(c, pt - s0 - 1)));
+                NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
+            } else if (e - 1 == s0) {
+                NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
+            }
+            NB_TRY(vjp(c, pt == 0 ? 0.5 * dt : dt));
+        }
+    }
+    NB_TRY(download_r(c, c->adj_lx, 3 * n, gx0, st));
+    NB_TRY(download_r(c, c->adj_lv, 3 * n, gv0, st + 3 * n));
+    NB_TRY(download_r(c, c->adj_gq, n, gq, st + 6 * n));
+    NB_TRY(download_r(c, c->adj_gm, n, gm, st + 7 * n));
+    // back to the recorded run's final state
+    NB_TRY(snap_load(c, final_slot(c)));
+    c->time = c->ck_t0 + N * dt;
+    NB_CU(c, cudaStreamSynchronize(c->st));
+    return NBODY_OK;
+}
+
+}  // extern "C"

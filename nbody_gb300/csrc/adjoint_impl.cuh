@@ -1,0 +1,435 @@
+// Discrete adjoint of one FMM force evaluation (vector-Jacobian product),
+// with the tree and every interaction list frozen at the forward evaluation.
+//
+// For S = sum_i mu_i . a_i with a_i = G q_i/m_i E_i the product is taken
+// operator by operator, in reverse:
+//   near field  gx_k += sum_l T(r_kl) (q_k nu_l - q_l nu_k),  gq_k += nu_l . K(x_k - x_l)
+//               (nu_i = G q_i/m_i mu_i, K(r) = r/s^3/2, T = dK/dr); the near-field pair set
+//               is symmetric, so both the target and the source role of particle k are
+//               gathered in k's own list: no scatter, no atomics;
+//   L2P         gx_k += H(L) nu_k (Hessian of the local expansion) and
+//               lamL(leaf) = sum_k sum_d nu_k,d y^(n-e_d)/(n-e_d)!;
+//   L2L^T       an M2M pass on lamL (children -> parent, same shift operator);
+//   M2L^T       the forward M2L kernel run on lamL over the same (symmetric) far-field
+//               lists gives lamM (the operator's transpose has the forward form);
+//   M2M^T       an L2L pass on lamM (parent -> children);
+//   P2M^T       gq_k += psi_lamM(y_k), gx_k += q_k grad psi_lamM(y_k) (an L2P of lamM);
+//   prefactor   gq_k += mu_k . a_k / q_k, gm_k -= mu_k . a_k / m_k.
+// Cell centres are geometric, so M2M, M2L and L2L are constant linear maps.
+#pragma once
+
+namespace nbfmm {
+
+struct AdjArgs {
+    int64_t n;
+    const uint32_t* ids;              // sorted row -> input index
+    const void *lv, *q, *m, *ax, *ay, *az;   // R*: lv (input order, 3n), q/m/a (sorted)
+    double c, G;                      // mu = c * lv
+    void* nu;                         // S4* (sorted)
+    void *gx, *gq, *gm;               // R* accumulators (input order; gx 3n)
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_adj_prep(AdjArgs A) {
+    typedef typename Prec<MODE>::R R;
+    typedef typename Prec<MODE>::S4 S4;
+    const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (i >= A.n) return;
+    const uint32_t id = A.ids[i];
+    const R* lv = (const R*)A.lv;
+    const R c = (R)A.c;
+    const R mx = c * lv[3 * id], my = c * lv[3 * id + 1], mz = c * lv[3 * id + 2];
+    const R qi = ((const R*)A.q)[i], mi = ((const R*)A.m)[i];
+    const R f = (R)A.G * qi / mi;
+    S4 v;
+    v.x = (decltype(v.x))(f * mx); v.y = (decltype(v.y))(f * my); v.z = (decltype(v.z))(f * mz); v.w = 0;
+    ((S4*)A.nu)[i] = v;
+    const R mua = mx * ((const R*)A.ax)[i] + my * ((const R*)A.ay)[i] + mz * ((const R*)A.az)[i];
+    if (qi != R(0)) ((R*)A.gq)[id] += mua / qi;
+    ((R*)A.gm)[id] -= mua / mi;
+}
+
+// transpose of L2P: lamL_n of each leaf (lane per coefficient, like k_p2m)
+template <int MODE, int P>
+__global__ void __launch_bounds__(128) k_adj_l2pT(int64_t nleaves, const uint32_t* __restrict__ leaves,
+                                                  const NodeRec* __restrict__ nodes,
+                                                  const typename Prec<MODE>::S4* __restrict__ src,
+                                                  const typename Prec<MODE>::S4* __restrict__ nu,
+                                                  typename Prec<MODE>::H* __restrict__ lamL, float* __restrict__ lamL32) {
+    typedef typename Prec<MODE>::S S;
+    typedef typename Prec<MODE>::H H;
+    constexpr int T = nb_terms<P>::value;
+    constexpr int TM = nb_tm<P>::value;
+    constexpr int NPL = (T + 31) / 32;
+    __shared__ S pw[4][32][3][P + 1];
+    __shared__ S sn[4][32][3];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int64_t w = (int64_t)blockIdx.x * 4 + wib;
+    if (w >= nleaves) return;
+    const uint32_t k = leaves[w];
+    const NodeRec nd = nodes[k];
+    int ex[NPL][3];
+    S acc[NPL];
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        acc[j] = S(0);
+        const int a = lane + 32 * j, aa = a < T ? a : 0;
+        ex[j][0] = nb_mi[aa][0]; ex[j][1] = nb_mi[aa][1]; ex[j][2] = nb_mi[aa][2];
+    }
+    const uint32_t end = nd.begin + nd.count;
+    for (uint32_t base = nd.begin; base < end; base += 32) {
+        const uint32_t i = base + lane;
+        if (i < end) {
+            const typename Prec<MODE>::S4 y = src[i], v = nu[i];
+            const S yy[3] = {y.x, y.y, y.z};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                S p = S(1);
+#pragma unroll
+                for (int e = 0; e <= P; ++e) { pw[wib][lane][d][e] = p; p *= yy[d]; }
+            }
+            sn[wib][lane][0] = v.x; sn[wib][lane][1] = v.y; sn[wib][lane][2] = v.z;
+        }
+        __syncwarp();
+        const int cnt = end - base < 32 ? (int)(end - base) : 32;
+        for (int jj = 0; jj < cnt; ++jj) {
+#pragma unroll
+            for (int j = 0; j < NPL; ++j) {
+                const int nx = ex[j][0], ny = ex[j][1], nz = ex[j][2];
+                S t = S(0);
+                if (nx) t = nb_fma(sn[wib][jj][0] * (S)nx, pw[wib][jj][0][nx - 1] * pw[wib][jj][1][ny] * pw[wib][jj][2][nz], t);
+                if (ny) t = nb_fma(sn[wib][jj][1] * (S)ny, pw[wib][jj][0][nx] * pw[wib][jj][1][ny - 1] * pw[wib][jj][2][nz], t);
+                if (nz) t = nb_fma(sn[wib][jj][2] * (S)nz, pw[wib][jj][0][nx] * pw[wib][jj][1][ny] * pw[wib][jj][2][nz - 1], t);
+                acc[j] += t;
+            }
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        const int a = lane + 32 * j;
+        if (a < T) {
+            const H v = (H)acc[j] * (H)nb_invfact[a];
+            lamL[(int64_t)k * TM + a] = v;
+            if (lamL32) lamL32[(int64_t)k * TM + a] = (float)v;
+        }
+    }
+}
+
+struct AdjP2PArgs {
+    const uint32_t* leaves;
+    int64_t nleaves;
+    const NodeRec* nodes;
+    const BoxDev* box;
+    const void* src;          // S4* (offset from the leaf centre, q)
+    const void* nu;           // S4*
+    const void* L;            // H*: forward local expansions (stride T)
+    const void* lamM;         // H*: adjoint multipoles (stride T)
+    const uint32_t *p2p_off, *p2p_cnt, *p2p_list;
+    const uint32_t* work_off;
+    int64_t nwork;
+    const uint32_t* part_off;
+    void* part;               // R[4] per (chunk, target)
+    const uint32_t* ids;
+    void *gx, *gq;            // R* accumulators (input order)
+    double eps2;
+};
+
+// far-field part of the adjoint at one particle + accumulation into the input-order sums
+template <int MODE, int P>
+__device__ __forceinline__ void adj_epilogue(const AdjP2PArgs& A, uint32_t i, const typename Prec<MODE>::S* sL,
+                                             const typename Prec<MODE>::S* sM, typename Prec<MODE>::S4 yi,
+                                             typename Prec<MODE>::S4 ni, typename Prec<MODE>::R gx,
+                                             typename Prec<MODE>::R gy, typename Prec<MODE>::R gz,
+                                             typename Prec<MODE>::R gq) {
+    typedef typename Prec<MODE>::R R;
+    typedef typename Prec<MODE>::S S;
+    S hx, hy, hz;
+    Ops<S, P>::l2p_hess(sL, yi.x, yi.y, yi.z, ni.x, ni.y, ni.z, hx, hy, hz);
+    S fx, fy, fz, fp;
+    Ops<S, P>::l2p(sM, yi.x, yi.y, yi.z, fx, fy, fz, fp);
+    const uint32_t id = A.ids[i];
+    R* GX = (R*)A.gx;
+    R* GQ = (R*)A.gq;
+    const R qi = (R)yi.w;
+    GX[3 * id] += gx + (R)hx + qi * (R)fx;
+    GX[3 * id + 1] += gy + (R)hy + qi * (R)fy;
+    GX[3 * id + 2] += gz + (R)hz + qi * (R)fz;
+    GQ[id] += gq + (R)fp;
+}
+
+constexpr int ADJ_WARPS = 4;
+
+template <int MODE, int P>
+__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_p2p(AdjP2PArgs A) {
+    typedef typename Prec<MODE>::R R;
+    typedef typename Prec<MODE>::S S;
+    typedef typename Prec<MODE>::H H;
+    typedef typename Prec<MODE>::S4 S4;
+    constexpr int T = nb_terms<P>::value;
+    constexpr bool KH = Prec<MODE>::kahan;
+    __shared__ S4 tx[ADJ_WARPS][4][P2P_TILE];
+    __shared__ S4 tn[ADJ_WARPS][4][P2P_TILE];
+    __shared__ S sL[ADJ_WARPS][T];
+    __shared__ S sM[ADJ_WARPS][T];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int64_t w = (int64_t)blockIdx.x * ADJ_WARPS + wib;
+    if (w >= A.nwork) return;
+    int64_t lo = 0, hi = A.nleaves;
+    while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (A.work_off[mid] <= (uint32_t)w) lo = mid; else hi = mid;
+    }
+    const int64_t li = lo;
+    const uint32_t chunk = (uint32_t)w - A.work_off[li];
+    const uint32_t nchunk = A.work_off[li + 1] - A.work_off[li];
+    const uint32_t k = A.leaves[li];
+    const NodeRec nt = A.nodes[k];
+    const double unit = A.box->unit;
+    const S4* src = (const S4*)A.src;
+    const S4* nu = (const S4*)A.nu;
+    if (nchunk == 1) {
+        const H* Lg = (const H*)A.L;
+        const H* Mg = (const H*)A.lamM;
+        for (int a = lane; a < T; a += 32) {
+            sL[wib][a] = (S)Lg[(int64_t)k * T + a];
+            sM[wib][a] = (S)Mg[(int64_t)k * T + a];
+        }
+    }
+    const uint32_t cnt_t = nt.count;
+    const int CT = cnt_t <= 8 ? 8 : cnt_t <= 16 ? 16 : 32;
+    const int NG = 32 / CT, grp = lane / CT, gl = lane % CT;
+    const uint32_t loff = A.p2p_off[k], lcnt = A.p2p_cnt[k];
+    const uint32_t s_lo = chunk * P2P_CHUNK, s_hi = min(lcnt, s_lo + P2P_CHUNK);
+    const S eps2 = (S)A.eps2;
+    const bool guard = !(A.eps2 > 0.0);
+    __syncwarp();
+    for (uint32_t tc = 0; tc < cnt_t; tc += CT) {
+        const uint32_t ti = tc + gl;
+        const bool tv = ti < cnt_t;
+        const uint32_t i = nt.begin + (tv ? ti : 0);
+        const S4 yk = src[i], nk = nu[i];
+        S gx = 0, gy = 0, gz = 0, gq = 0, cx = 0, cy = 0, cz = 0, cq = 0;
+        for (uint32_t base = s_lo; base < s_hi; base += 32) {
+            const uint32_t nb = min(32u, s_hi - base);
+            uint32_t my_beg = 0, my_cnt = 0;
+            S my_dx = 0, my_dy = 0, my_dz = 0;
+            if ((uint32_t)lane < nb) {
+                const NodeRec sn = A.nodes[A.p2p_list[loff + base + lane]];
+                my_beg = sn.begin;
+                my_cnt = sn.count;
+                double ddx, ddy, ddz;
+                disp(sn, nt, unit, ddx, ddy, ddz);
+                my_dx = (S)ddx; my_dy = (S)ddy; my_dz = (S)ddz;
+            }
+            const uint32_t rounds = (nb + NG - 1) / NG;
+            for (uint32_t rr = 0; rr < rounds; ++rr) {
+                const uint32_t q = rr * NG + grp;
+                const uint32_t qs = q & 31;
+                const uint32_t beg = __shfl_sync(0xffffffffu, my_beg, qs);
+                const uint32_t scnt0 = __shfl_sync(0xffffffffu, my_cnt, qs);
+                const S dx = __shfl_sync(0xffffffffu, my_dx, qs), dy = __shfl_sync(0xffffffffu, my_dy, qs),
+                        dz = __shfl_sync(0xffffffffu, my_dz, qs);
+                const uint32_t scnt = q < nb ? scnt0 : 0u;
+                uint32_t mx = scnt;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                const S xk = yk.x - dx, yk_ = yk.y - dy, zk = yk.z - dz;
+                for (uint32_t sb = 0; sb < mx; sb += P2P_TILE) {
+                    for (int e = gl; e < P2P_TILE; e += CT) {
+                        const uint32_t j = sb + e;
+                        S4 a, b;
+                        if (j < scnt) { a = src[beg + j]; b = nu[beg + j]; }
+                        else { a.x = 0; a.y = 0; a.z = 0; a.w = 0; b = a; }
+                        tx[wib][grp][e] = a;
+                        tn[wib][grp][e] = b;
+                    }
+                    __syncwarp();
+                    const int nj = scnt > sb ? min((int)(scnt - sb), P2P_TILE) : 0;
+                    S px = 0, py = 0, pz = 0, pq = 0;
+                    for (int e = 0; e < nj; ++e) {
+                        const S4 sx = tx[wib][grp][e], sv = tn[wib][grp][e];
+                        const S rx = sx.x - xk, ry = sx.y - yk_, rz = sx.z - zk;
+                        S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
+                        if (guard) s2 = s2 > S(0) ? s2 : S(1e30);
+                        const S inv = nb_rsqrt(s2), inv2 = inv * inv, inv3 = inv2 * inv, inv5 = inv3 * inv2;
+                        const S wx = yk.w * sv.x - sx.w * nk.x, wy = yk.w * sv.y - sx.w * nk.y,
+                                wz = yk.w * sv.z - sx.w * nk.z;
+                        const S t3 = S(3) * nb_fma(rx, wx, nb_fma(ry, wy, rz * wz)) * inv5;
+                        px = nb_fma(wx, inv3, nb_fma(-rx, t3, px));
+                        py = nb_fma(wy, inv3, nb_fma(-ry, t3, py));
+                        pz = nb_fma(wz, inv3, nb_fma(-rz, t3, pz));
+                        pq = nb_fma(-nb_fma(sv.x, rx, nb_fma(sv.y, ry, sv.z * rz)), inv3, pq);
+                    }
+                    if (KH) {
+                        kahan_add(gx, cx, px); kahan_add(gy, cy, py); kahan_add(gz, cz, pz); kahan_add(gq, cq, pq);
+                    } else {
+                        gx += px; gy += py; gz += pz; gq += pq;
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+        R Gx = (R)gx - (R)cx, Gy = (R)gy - (R)cy, Gz = (R)gz - (R)cz, Gq = (R)gq - (R)cq;
+        for (int o = CT; o < 32; o <<= 1) {
+            Gx += shfl_xor_t(Gx, o); Gy += shfl_xor_t(Gy, o); Gz += shfl_xor_t(Gz, o); Gq += shfl_xor_t(Gq, o);
+        }
+        if (grp == 0 && tv) {
+            if (nchunk == 1) {
+                adj_epilogue<MODE, P>(A, i, sL[wib], sM[wib], yk, nk, Gx, Gy, Gz, Gq);
+            } else {
+                R* pt = (R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)chunk * cnt_t + ti);
+                pt[0] = Gx; pt[1] = Gy; pt[2] = Gz; pt[3] = Gq;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <int MODE, int P>
+__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_p2p_final(AdjP2PArgs A) {
+    typedef typename Prec<MODE>::R R;
+    typedef typename Prec<MODE>::S S;
+    typedef typename Prec<MODE>::H H;
+    typedef typename Prec<MODE>::S4 S4;
+    constexpr int T = nb_terms<P>::value;
+    __shared__ S sL[ADJ_WARPS][T];
+    __shared__ S sM[ADJ_WARPS][T];
+    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int64_t li = (int64_t)blockIdx.x * ADJ_WARPS + wib;
+    if (li >= A.nleaves) return;
+    const uint32_t nchunk = A.work_off[li + 1] - A.work_off[li];
+    if (nchunk <= 1) return;
+    const uint32_t k = A.leaves[li];
+    const NodeRec nt = A.nodes[k];
+    const H* Lg = (const H*)A.L;
+    const H* Mg = (const H*)A.lamM;
+    for (int a = lane; a < T; a += 32) {
+        sL[wib][a] = (S)Lg[(int64_t)k * T + a];
+        sM[wib][a] = (S)Mg[(int64_t)k * T + a];
+    }
+    __syncwarp();
+    const S4* src = (const S4*)A.src;
+    const S4* nu = (const S4*)A.nu;
+    for (uint32_t ti = lane; ti < nt.count; ti += 32) {
+        R e[4] = {0, 0, 0, 0};
+        for (uint32_t c = 0; c < nchunk; ++c) {
+            const R* pt = (const R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)c * nt.count + ti);
+            e[0] += pt[0]; e[1] += pt[1]; e[2] += pt[2]; e[3] += pt[3];
+        }
+        const uint32_t i = nt.begin + ti;
+        adj_epilogue<MODE, P>(A, i, sL[wib], sM[wib], src[i], nu[i], e[0], e[1], e[2], e[3]);
+    }
+}
+
+// host: one VJP at the last evaluated positions; mu = c * lv (input order)
+template <int MODE, int P>
+int force_vjp(nbody_ctx* c, double coef) {
+    typedef typename Prec<MODE>::R R;
+    typedef typename Prec<MODE>::H H;
+    typedef typename Prec<MODE>::S4 S4;
+    constexpr int T = nb_terms<P>::value;
+    constexpr int TM = nb_tm<P>::value;
+    const int64_t nn = c->nnodes, n = c->n, nl = c->nleaves;
+    const int cur = c->cur;
+    const BoxDev* box = DP<BoxDev>(c->box);
+    NB_TRY(nb_grow(c, c->adj_nu, sizeof(S4) * n));
+    NB_TRY(nb_grow(c, c->adj_lamL, sizeof(H) * TM * nn));
+    if (MODE == NBODY_PREC_MIXED) NB_TRY(nb_grow(c, c->adj_lamL32, sizeof(float) * TM * nn));
+    NB_TRY(nb_grow(c, c->adj_lamM, sizeof(H) * T * nn));
+    float* lamL32 = MODE == NBODY_PREC_MIXED ? DP<float>(c->adj_lamL32) : nullptr;
+
+    AdjArgs A;
+    A.n = n;
+    A.ids = DP<uint32_t>(c->id[cur]);
+    A.lv = c->adj_lv.p;
+    A.q = c->q[cur].p; A.m = c->m[cur].p; A.ax = c->ax[cur].p; A.ay = c->ay[cur].p; A.az = c->az[cur].p;
+    A.c = coef;
+    A.G = c->prm.G;
+    A.nu = c->adj_nu.p;
+    A.gx = c->adj_lx.p; A.gq = c->adj_gq.p; A.gm = c->adj_gm.p;
+    k_adj_prep<MODE><<<(unsigned)((n + 255) / 256), 256, 0, c->st>>>(A);
+    NB_LAUNCHED(c, "adj_prep");
+    c->launches += 1;
+    k_adj_l2pT<MODE, P><<<(unsigned)((nl + 3) / 4), 128, 0, c->st>>>(
+        nl, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes), DP<S4>(c->src), DP<S4>(c->adj_nu), DP<H>(c->adj_lamL),
+        lamL32);
+    NB_LAUNCHED(c, "adj_l2pT");
+    c->launches += 1;
+    for (int l = c->depth - 1; l >= 0; --l) {
+        const int lo = c->level_start[l], hi = c->level_start[l + 1];
+        if (hi <= lo) continue;
+        k_m2m<MODE, P><<<(unsigned)((hi - lo + 3) / 4), 128, 0, c->st>>>(lo, hi, DP<NodeRec>(c->nodes), box,
+                                                                         DP<H>(c->adj_lamL), lamL32);
+        NB_LAUNCHED(c, "adj_l2lT");
+        c->launches += 1;
+    }
+    {
+        M2LArgs B;
+        B.nodes = DP<NodeRec>(c->nodes);
+        B.box = box;
+        B.Mm2l = MODE == NBODY_PREC_MIXED ? (const void*)lamL32 : (const void*)c->adj_lamL.p;
+        B.L = c->adj_lamM.p;
+        B.m2l_off = DP<uint32_t>(c->m2l_off); B.m2l_cnt = DP<uint32_t>(c->m2l_cnt);
+        B.m2l_list = DP<uint32_t>(c->m2l_list);
+        B.eps2 = c->prm.eps * c->prm.eps;
+        B.nnodes = nn;
+        B.info = DP<int32_t>(c->info);
+        constexpr int W = M2LSmem<MODE, P>::warps;
+        const size_t smem = (size_t)W * M2LSmem<MODE, P>::per_warp;
+        NB_CU(c, cudaFuncSetAttribute(k_m2l<MODE, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_m2l<MODE, P><<<(unsigned)((nn + W - 1) / W), 32 * W, smem, c->st>>>(B);
+        NB_LAUNCHED(c, "adj_m2lT");
+        c->launches += 1;
+    }
+    for (int r = 1; r <= c->depth; ++r) {
+        const int lo = c->level_start[r], hi = c->level_start[r + 1];
+        if (hi <= lo) continue;
+        k_l2l<MODE, P><<<(unsigned)((hi - lo + 3) / 4), 128, 0, c->st>>>(lo, hi, DP<NodeRec>(c->nodes), box,
+                                                                         DP<H>(c->adj_lamM));
+        NB_LAUNCHED(c, "adj_m2mT");
+        c->launches += 1;
+    }
+    AdjP2PArgs C;
+    C.leaves = DP<uint32_t>(c->leaves);
+    C.nleaves = nl;
+    C.nodes = DP<NodeRec>(c->nodes);
+    C.box = box;
+    C.src = c->src.p;
+    C.nu = c->adj_nu.p;
+    C.L = c->L.p;
+    C.lamM = c->adj_lamM.p;
+    C.p2p_off = DP<uint32_t>(c->p2p_off); C.p2p_cnt = DP<uint32_t>(c->p2p_cnt); C.p2p_list = DP<uint32_t>(c->p2p_list);
+    C.work_off = DP<uint32_t>(c->p2p_work_off);
+    C.nwork = (uint32_t)c->h_info[INFO_P2P_WORK];
+    C.part_off = DP<uint32_t>(c->p2p_part_off);
+    C.part = c->p2p_part.p;
+    C.ids = DP<uint32_t>(c->id[cur]);
+    C.gx = c->adj_lx.p;
+    C.gq = c->adj_gq.p;
+    C.eps2 = c->prm.eps * c->prm.eps;
+    const int64_t npart = (uint32_t)c->h_info[INFO_P2P_PART];
+    k_adj_p2p<MODE, P><<<(unsigned)((C.nwork + ADJ_WARPS - 1) / ADJ_WARPS), 32 * ADJ_WARPS, 0, c->st>>>(C);
+    if (npart)
+        k_adj_p2p_final<MODE, P><<<(unsigned)((nl + ADJ_WARPS - 1) / ADJ_WARPS), 32 * ADJ_WARPS, 0, c->st>>>(C);
+    NB_LAUNCHED(c, "adj_p2p");
+    c->launches += npart ? 2 : 1;
+    return NBODY_OK;
+}
+
+template <int MODE>
+int vjp_dispatch(nbody_ctx* c, double coef) {
+    switch (c->prm.order) {
+        case 1: return force_vjp<MODE, 1>(c, coef);
+        case 2: return force_vjp<MODE, 2>(c, coef);
+        case 3: return force_vjp<MODE, 3>(c, coef);
+        case 4: return force_vjp<MODE, 4>(c, coef);
+        case 5: return force_vjp<MODE, 5>(c, coef);
+        case 6: return force_vjp<MODE, 6>(c, coef);
+        case 7: return force_vjp<MODE, 7>(c, coef);
+        case 8: return force_vjp<MODE, 8>(c, coef);
+        default: return nb_fail(c, NBODY_ERR_INVALID, "order must be 1..8");
+    }
+}
+
+}  // namespace nbfmm

@@ -173,9 +173,12 @@ int fmm(nbody_ctx* c, int integ, bool want_pot) {
     }
 }
 
+}  // namespace
+
 // one force evaluation at the current positions, with an optional integrator epilogue
-int evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
+int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
     c->launches = 0;
+    c->tree_at_final = false;
     if (c->timing) cudaEventRecord(c->ev[0], c->st);
     NB_TRY(nb_begin_step(c, kdk));
     if (c->timing) cudaEventRecord(c->ev[1], c->st);
@@ -194,6 +197,8 @@ int evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
     }
     return NBODY_OK;
 }
+
+namespace {
 
 template <typename R>
 int diag_t(nbody_ctx* c, double* out) {
@@ -287,7 +292,8 @@ int nbody_destroy(nbody_ctx* c) {
                       &c->p2p_part, &c->hist, &c->hist_scan, &c->scan_part, &c->cpl, &c->wnd, &c->leaflvl, &c->nc, &c->pfx,
                       &c->nodes, &c->leafflag, &c->leafpfx, &c->leaves, &c->M, &c->M32, &c->L, &c->src, &c->pend_off,
                       &c->pend_cnt, &c->p2p_off, &c->p2p_cnt, &c->pend_list, &c->p2p_list, &c->m2l_off, &c->m2l_cnt,
-                      &c->m2l_list, &c->stage, &c->diag, &c->info, &c->box, &c->bbox})
+                      &c->m2l_list, &c->stage, &c->diag, &c->info, &c->box, &c->bbox, &c->adj_lx, &c->adj_lv,
+                      &c->adj_gq, &c->adj_gm, &c->adj_nu, &c->adj_lamL, &c->adj_lamL32, &c->adj_lamM, &c->snaps})
         release(*b);
     if (c->h_info) cudaFreeHost(c->h_info);
     for (int i = 0; i < 16; ++i)
@@ -330,6 +336,7 @@ int nbody_set_state(nbody_ctx* c, int64_t n, const double* pos, const double* ve
     NB_CU(c, cudaStreamSynchronize(c->st));
     c->time = 0.0;
     c->have_acc = acc != nullptr;
+    c->ck_steps = 0;
     return NBODY_OK;
 }
 
@@ -360,15 +367,16 @@ int nbody_step(nbody_ctx* c, int nsteps, double* t_out) {
     if (c->n == 0) return nb_fail(c, NBODY_ERR_STATE, "no particles");
     if (nsteps < 0) return nb_fail(c, NBODY_ERR_INVALID, "nsteps must be >= 0");
     NB_CU(c, cudaSetDevice(c->device));
+    if (nsteps > 0) c->ck_steps = 0;
     for (int s = 0; s < nsteps; ++s) {
         if (c->prm.integrator == NBODY_INTEG_LEAPFROG) {
             if (!c->have_acc) {
-                NB_TRY(evaluate(c, 0, NB_INTEG_NONE, false));
+                NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
                 c->have_acc = true;
             }
-            NB_TRY(evaluate(c, 1, NB_INTEG_KDK_CLOSE, false));
+            NB_TRY(nb_evaluate(c, 1, NB_INTEG_KDK_CLOSE, false));
         } else {
-            NB_TRY(evaluate(c, 0, NB_INTEG_EULER, false));
+            NB_TRY(nb_evaluate(c, 0, NB_INTEG_EULER, false));
             c->have_acc = false;
         }
         c->time += c->prm.dt;
@@ -382,7 +390,7 @@ int nbody_compute_forces(nbody_ctx* c, double* acc, double* pot) {
     if (!c) return NBODY_ERR_INVALID;
     if (c->n == 0) return nb_fail(c, NBODY_ERR_STATE, "no particles");
     NB_CU(c, cudaSetDevice(c->device));
-    NB_TRY(evaluate(c, 0, NB_INTEG_NONE, pot != nullptr));
+    NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, pot != nullptr));
     c->have_acc = c->prm.integrator == NBODY_INTEG_LEAPFROG;
     if (acc || pot) {
         NB_TRY(fetch(c, 1));
@@ -399,7 +407,7 @@ int nbody_diagnostics(nbody_ctx* c, double* out) {
     if (!c || !out) return NBODY_ERR_INVALID;
     if (c->n == 0) return nb_fail(c, NBODY_ERR_STATE, "no particles");
     NB_CU(c, cudaSetDevice(c->device));
-    NB_TRY(evaluate(c, 0, NB_INTEG_NONE, true));
+    NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, true));
     c->have_acc = c->prm.integrator == NBODY_INTEG_LEAPFROG;
     return c->rsz == 4 ? diag_t<float>(c, out) : diag_t<double>(c, out);
 }

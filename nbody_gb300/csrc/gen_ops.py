@@ -182,6 +182,30 @@ def gen_l2p(p, o):
     o.append("  }")
 
 
+def gen_l2p_hess(p, o):
+    """h = H nu with H_de = sum_{|k| <= p-2} L[k + e_d + e_e] y^k/k! (Hessian of the
+    local expansion at y), used by the adjoint of L2P."""
+    o.append("  static __device__ __forceinline__ void l2p_hess(const S* __restrict__ L, S x, S y, S z, S nx, S ny, "
+             "S nz, S& hx, S& hy, S& hz) {")
+    if p < 2:
+        o.append("    hx = S(0); hy = S(0); hz = S(0);")
+        o.append("  }")
+        return
+    o.append(f"    S Y[{T(p - 2)}];")
+    o.append("    mono_lo(x, y, z, Y);")
+    names = {(0, 0): "xx", (0, 1): "xy", (0, 2): "xz", (1, 1): "yy", (1, 2): "yz", (2, 2): "zz"}
+    E = [(1, 0, 0), (0, 1, 0), (0, 0, 1)]
+    for (d, e), nm in names.items():
+        o.append(f"    S h{nm} = L[{idx(add(E[d], E[e]))}];")
+    for k in terms(p - 2)[1:]:
+        for (d, e), nm in names.items():
+            o.append(f"    h{nm} = nb_fma(L[{idx(add(k, add(E[d], E[e])))}], Y[{idx(k)}], h{nm});")
+    o.append("    hx = hxx * nx + hxy * ny + hxz * nz;")
+    o.append("    hy = hxy * nx + hyy * ny + hyz * nz;")
+    o.append("    hz = hxz * nx + hyz * ny + hzz * nz;")
+    o.append("  }")
+
+
 def shift_tables(p):
     ts = terms(p)
     m2m, l2l = [], []
@@ -212,8 +236,13 @@ def main():
         gen_m2l(p, o)
         gen_m2l_v(p, o)
         gen_mono(p, o)
+        if p >= 2:
+            lo = []
+            gen_mono(p - 2, lo, name="mono_lo")
+            o.extend(lo)
         gen_p2m(p, o)
         gen_l2p(p, o)
+        gen_l2p_hess(p, o)
         o.append("};")
     # shift tables: (out, in, mono) triples, grouped by output index
     for p in range(1, PMAX + 1):

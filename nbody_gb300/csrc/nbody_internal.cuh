@@ -101,6 +101,15 @@ struct nbody_ctx {
     int32_t* h_info = nullptr;
     double* h_box = nullptr;
 
+    // adjoint (input-order accumulators, adjoint expansions, trajectory snapshots)
+    DevBuf adj_lx, adj_lv, adj_gq, adj_gm, adj_nu, adj_lamL, adj_lamL32, adj_lamM;
+    DevBuf snaps;                  // sorted-state snapshots: checkpoints, segment scratch, final state
+    size_t snap_bytes = 0;         // bytes of one snapshot
+    int ck_steps = 0;              // steps of the recorded run (0: nothing recorded)
+    int ck_every = 0;              // checkpoint spacing of the recorded run
+    double ck_t0 = 0.0;            // simulated time at its start
+    bool tree_at_final = false;    // the last evaluation was the recorded run's final one
+
     // per-phase timing
     bool timing = false;
     cudaEvent_t ev[16] = {};
@@ -137,10 +146,17 @@ int nb_begin_step(nbody_ctx* c, int kdk);
 int nb_sort_and_gather(nbody_ctx* c);
 int nb_build_tree(nbody_ctx* c);
 
+// one force evaluation at the current positions (api.cu); kdk = 1 applies the opening kick and drift first
+int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot);
+
 // fmm (fmm_*.cu)
 int nb_fmm_forces_fp32(nbody_ctx* c, int integ, bool want_pot);
 int nb_fmm_forces_mixed(nbody_ctx* c, int integ, bool want_pot);
 int nb_fmm_forces_fp64(nbody_ctx* c, int integ, bool want_pot);
+// adjoint of the last force evaluation (fmm_*.cu): mu = coef * adj_lv, accumulated into adj_lx/adj_gq/adj_gm
+int nb_fmm_vjp_fp32(nbody_ctx* c, double coef);
+int nb_fmm_vjp_mixed(nbody_ctx* c, double coef);
+int nb_fmm_vjp_fp64(nbody_ctx* c, double coef);
 
 // integration modes of the force epilogue
 enum { NB_INTEG_NONE = 0, NB_INTEG_KDK_CLOSE = 1, NB_INTEG_EULER = 2 };

@@ -196,6 +196,36 @@ class CudaSimulation:
         check(self._h, _lib.load().nbody_direct_forces(self._h, len(tg), ptr(tg), ptr(acc), ptr(pot)))
         return acc, pot
 
+    # -- adjoint ----------------------------------------------------------------
+    def force_vjp(self, mu):
+        """For S = sum_i mu_i . a_i at the current positions: (dS/dx (n,3), dS/dq (n,), dS/dm (n,)),
+        input order, tree and interaction lists held fixed."""
+        mu = np.ascontiguousarray(mu, dtype=np.float64).reshape(self.n, 3)
+        gx = np.empty((self.n, 3))
+        gq = np.empty(self.n)
+        gm = np.empty(self.n)
+        check(self._h, _lib.load().nbody_force_vjp(self._h, ptr(mu), ptr(gx), ptr(gq), ptr(gm)))
+        return gx, gq, gm
+
+    def forward_checkpointed(self, nsteps: int, every: int = 1) -> float:
+        """nsteps leapfrog steps, recording snapshots every `every` steps for backward()."""
+        t = C.c_double()
+        check(self._h, _lib.load().nbody_forward_checkpointed(self._h, int(nsteps), int(every), C.byref(t)))
+        return t.value
+
+    def backward(self, gx_final=None, gv_final=None):
+        """Reverse sweep of the recorded run: given dL/dx_N and dL/dv_N (n,3; None = 0), returns
+        (dL/dx_0, dL/dv_0, dL/dq, dL/dm) in input order."""
+        gxT = None if gx_final is None else np.ascontiguousarray(gx_final, dtype=np.float64).reshape(self.n, 3)
+        gvT = None if gv_final is None else np.ascontiguousarray(gv_final, dtype=np.float64).reshape(self.n, 3)
+        gx0 = np.empty((self.n, 3))
+        gv0 = np.empty((self.n, 3))
+        gq = np.empty(self.n)
+        gm = np.empty(self.n)
+        check(self._h, _lib.load().nbody_backward(self._h, ptr(gxT), ptr(gvT), ptr(gx0), ptr(gv0), ptr(gq),
+                                                  ptr(gm)))
+        return gx0, gv0, gq, gm
+
     def stats(self):
         out = np.zeros(7, np.int64)
         check(self._h, _lib.load().nbody_get_stats(self._h, ptr(out), 7))

@@ -288,6 +288,19 @@ void orc_destroy(orc_ctx* c) {
     free(c);
 }
 
+/* Replaces the particles' positions, charges and masses (input order; NULL
+   keeps the current values) while the tree and the interaction lists stay as
+   built: evaluations after this are the FMM with a frozen tree, whose
+   finite differences give the derivative the adjoint computes. */
+void orc_set_particles(orc_ctx* c, const double* pos, const double* q, const double* m) {
+    for (int64_t i = 0; i < c->n; ++i) {
+        uint32_t j = c->perm[i];
+        if (pos) memcpy(c->pos + 3 * i, pos + 3 * (int64_t)j, sizeof(double) * 3);
+        if (q) c->q[i] = q[j];
+        if (m) c->m[i] = m[j];
+    }
+}
+
 int64_t orc_nnodes(const orc_ctx* c) { return c->nnodes; }
 int orc_depth(const orc_ctx* c) { return c->depth; }
 
@@ -640,6 +653,112 @@ void orc_direct(int64_t n, const double* pos, const double* q, const double* m, 
         pthread_create(&th[t], NULL, direct_worker, &J[t]);
     }
     for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+}
+
+/* ------------------------------------------------------------------ */
+/* FP64 direct-sum force adjoint (vector-Jacobian product)              */
+/* ------------------------------------------------------------------ */
+/* With a_i = G q_i/m_i sum_{j != i} q_j K(x_j - x_i), K(r) = r / s^(3/2),
+   s = |r|^2 + eps^2, returns for S = sum_i mu_i . a_i:
+     gx_k = dS/dx_k = sum_{l != k} T(x_l - x_k) (q_k nu_l - q_l nu_k),
+            T(r) = I / s^(3/2) - 3 r r^T / s^(5/2),  nu_i = G q_i/m_i mu_i
+     gq_k = dS/dq_k = sum_{l != k} nu_l . K(x_k - x_l) + G/m_k mu_k . E_k
+     gm_k = dS/dm_k = -G q_k/m_k^2 mu_k . E_k                             */
+typedef struct {
+    int64_t n; const double *pos, *q, *m, *nu, *mu; double eps2, G;
+    double *gx, *gq, *gm; int64_t lo, hi;
+} vjp_job;
+
+static void* vjp_worker(void* arg) {
+    vjp_job* J = (vjp_job*)arg;
+    for (int64_t k = J->lo; k < J->hi; ++k) {
+        const double xk = J->pos[3 * k], yk = J->pos[3 * k + 1], zk = J->pos[3 * k + 2];
+        const double qk = J->q[k];
+        const double* nk = J->nu + 3 * k;
+        double g[3] = {0, 0, 0}, gq = 0, E[3] = {0, 0, 0};
+        for (int64_t l = 0; l < J->n; ++l) {
+            if (l == k) continue;
+            const double rx = J->pos[3 * l] - xk, ry = J->pos[3 * l + 1] - yk, rz = J->pos[3 * l + 2] - zk;
+            const double s = rx * rx + ry * ry + rz * rz + J->eps2;
+            if (s == 0.0) continue;
+            const double inv = 1.0 / sqrt(s), inv3 = inv * inv * inv, inv5 = inv3 * inv * inv;
+            const double* nl = J->nu + 3 * l;
+            const double ql = J->q[l];
+            const double w[3] = {qk * nl[0] - ql * nk[0], qk * nl[1] - ql * nk[1], qk * nl[2] - ql * nk[2]};
+            const double rw = rx * w[0] + ry * w[1] + rz * w[2];
+            g[0] += w[0] * inv3 - 3.0 * rx * rw * inv5;
+            g[1] += w[1] * inv3 - 3.0 * ry * rw * inv5;
+            g[2] += w[2] * inv3 - 3.0 * rz * rw * inv5;
+            gq -= (nl[0] * rx + nl[1] * ry + nl[2] * rz) * inv3;
+            E[0] += ql * rx * inv3; E[1] += ql * ry * inv3; E[2] += ql * rz * inv3;
+        }
+        const double* mk = J->mu + 3 * k;
+        const double muE = mk[0] * E[0] + mk[1] * E[1] + mk[2] * E[2];
+        J->gx[3 * k] = g[0]; J->gx[3 * k + 1] = g[1]; J->gx[3 * k + 2] = g[2];
+        J->gq[k] = gq + J->G / J->m[k] * muE;
+        J->gm[k] = -J->G * qk / (J->m[k] * J->m[k]) * muE;
+    }
+    return NULL;
+}
+
+void orc_direct_vjp(int64_t n, const double* pos, const double* q, const double* m, double eps, double G,
+                    const double* mu, double* gx, double* gq, double* gm, int nthreads) {
+    double* nu = (double*)malloc(sizeof(double) * 3 * (n ? n : 1));
+    for (int64_t i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) nu[3 * i + d] = G * q[i] / m[i] * mu[3 * i + d];
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 64) nthreads = 64;
+    pthread_t th[64];
+    vjp_job J[64];
+    for (int t = 0; t < nthreads; ++t) {
+        J[t] = (vjp_job){n, pos, q, m, nu, mu, eps * eps, G, gx, gq, gm, n * t / nthreads, n * (t + 1) / nthreads};
+        pthread_create(&th[t], NULL, vjp_worker, &J[t]);
+    }
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+    free(nu);
+}
+
+/* Adjoint of `steps` kick-drift-kick steps with direct-sum forces: given
+   gxT = dL/dx_N and gvT = dL/dv_N, returns dL/dx_0, dL/dv_0, dL/dq, dL/dm.
+   Reverse sweep: lv_{N-1/2} = lv_N, lx_N += dt/2 J_N^T lv_N; then for
+   n = N-1..0: lv_{n+1/2} += dt lx_{n+1} (drift), lx_n += c J_n^T lv_{n+1/2}
+   with c = dt (n >= 1) or dt/2 (n = 0) (kicks), parameters likewise. */
+void orc_leapfrog_adjoint(int64_t n, const double* pos0, const double* vel0, const double* q, const double* m,
+                          double eps, double G, double dt, int steps, const double* gxT, const double* gvT,
+                          double* gx0, double* gv0, double* gq, double* gm, int nthreads) {
+    size_t sz = 3 * (size_t)n;
+    double* xs = (double*)malloc(sizeof(double) * sz * (steps + 1));
+    double* v = (double*)malloc(sizeof(double) * sz);
+    double* acc = (double*)malloc(sizeof(double) * sz);
+    memcpy(xs, pos0, sizeof(double) * sz);
+    memcpy(v, vel0, sizeof(double) * sz);
+    orc_direct(n, xs, q, m, eps, G, 0, NULL, acc, NULL, nthreads);
+    for (int s = 0; s < steps; ++s) {
+        double* x0 = xs + sz * s;
+        double* x1 = xs + sz * (s + 1);
+        for (size_t i = 0; i < sz; ++i) { v[i] += 0.5 * dt * acc[i]; x1[i] = x0[i] + dt * v[i]; }
+        orc_direct(n, x1, q, m, eps, G, 0, NULL, acc, NULL, nthreads);
+        for (size_t i = 0; i < sz; ++i) v[i] += 0.5 * dt * acc[i];
+    }
+    double* lx = gx0;
+    double* lv = gv0;
+    memcpy(lx, gxT, sizeof(double) * sz);
+    memcpy(lv, gvT, sizeof(double) * sz);
+    for (int64_t i = 0; i < n; ++i) { gq[i] = 0; gm[i] = 0; }
+    double* mu = (double*)malloc(sizeof(double) * sz);
+    double* gx = (double*)malloc(sizeof(double) * sz);
+    double* tq = (double*)malloc(sizeof(double) * (n ? n : 1));
+    double* tm = (double*)malloc(sizeof(double) * (n ? n : 1));
+    for (int pt = steps; pt >= 0; --pt) {
+        if (pt < steps)
+            for (size_t i = 0; i < sz; ++i) lv[i] += dt * lx[i];      /* drift of step pt */
+        const double c = (pt == steps || pt == 0) ? 0.5 * dt : dt;
+        for (size_t i = 0; i < sz; ++i) mu[i] = c * lv[i];
+        orc_direct_vjp(n, xs + sz * pt, q, m, eps, G, mu, gx, tq, tm, nthreads);
+        for (size_t i = 0; i < sz; ++i) lx[i] += gx[i];
+        for (int64_t i = 0; i < n; ++i) { gq[i] += tq[i]; gm[i] += tm[i]; }
+    }
+    free(xs); free(v); free(acc); free(mu); free(gx); free(tq); free(tm);
 }
 
 /* ------------------------------------------------------------------ */

@@ -60,6 +60,8 @@ def lib():
     L.orc_get_list.argtypes = [C.c_void_p, C.c_int, _i32p]
     L.orc_fmm.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, _f64p, _f64p, C.c_void_p, C.c_void_p]
     L.orc_ref_forces_f32.argtypes = [C.c_void_p, C.c_float, _f32p, _f32p]
+    L.orc_set_particles.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.orc_set_particles.restype = None
     L.orc_direct.argtypes = [C.c_int64, _f64p, _f64p, _f64p, C.c_double, C.c_double, C.c_int64, C.c_void_p,
                              _f64p, C.c_void_p, C.c_int]
     L.orc_leapfrog.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _f64p, C.c_double, C.c_double, C.c_double,
@@ -71,6 +73,10 @@ def lib():
                                     C.c_int, C.c_int]
     L.orc_naive_rows.restype = C.c_int64
     L.orc_naive_rows.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int]
+    L.orc_direct_vjp.argtypes = [C.c_int64, _f64p, _f64p, _f64p, C.c_double, C.c_double, _f64p, _f64p, _f64p, _f64p,
+                                 C.c_int]
+    L.orc_leapfrog_adjoint.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _f64p, C.c_double, C.c_double, C.c_double,
+                                       C.c_int, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p, C.c_int]
     L.orc_morton_keys.argtypes = [C.c_int64, _f64p, _f64p, _u64p]
     L.orc_derivs.argtypes = [C.c_int, _f64p, C.c_double, _f64p]
     L.orc_nterms.restype = C.c_int
@@ -164,6 +170,14 @@ class Tree:
             raise RuntimeError("orc_fmm failed (traverse first; order in 1..10)")
         return acc[: 3 * self.n].reshape(-1, 3), pot[: self.n]
 
+    def set_particles(self, pos=None, q=None, m=None):
+        """New positions / charges / masses (input order) with the tree and lists kept (frozen tree)."""
+        keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)[: k * self.n].copy()
+                for a, k in ((pos, 3), (q, 1), (m, 1))]
+        ptrs = [None if a is None else a.ctypes.data_as(C.c_void_p) for a in keep]
+        lib().orc_set_particles(self._h, *ptrs)
+        return self
+
     def ref_forces_f32(self, eps=0.01):
         fl = np.zeros(3 * max(self.n, 1), np.float32)
         fn = np.zeros(3 * max(self.n, 1), np.float32)
@@ -225,6 +239,30 @@ def leapfrog(pos, vel, q, m, eps, G, dt, steps, nthreads=None):
     m = np.ascontiguousarray(m, dtype=np.float64)
     lib().orc_leapfrog(n, pos, vel, q, m, eps, G, dt, steps, acc, 0, nthreads or min(os.cpu_count() or 1, 32))
     return pos.reshape(-1, 3), vel.reshape(-1, 3), acc.reshape(-1, 3)
+
+
+def direct_vjp(pos, q, m, mu, eps=0.01, G=1.0, nthreads=None):
+    """FP64 direct-sum VJP of S = sum_i mu_i . a_i: (dS/dx, dS/dq, dS/dm)."""
+    pos = np.ascontiguousarray(pos, np.float64).reshape(-1)
+    n = pos.shape[0] // 3
+    gx, gq, gm = np.zeros(3 * n), np.zeros(n), np.zeros(n)
+    lib().orc_direct_vjp(n, pos, np.ascontiguousarray(q, np.float64), np.ascontiguousarray(m, np.float64), eps, G,
+                         np.ascontiguousarray(mu, np.float64).reshape(-1), gx, gq, gm,
+                         nthreads or min(os.cpu_count() or 1, 32))
+    return gx.reshape(-1, 3), gq, gm
+
+
+def leapfrog_adjoint(pos, vel, q, m, eps, G, dt, steps, gxT, gvT, nthreads=None):
+    """FP64 direct-sum leapfrog adjoint: (dL/dx0, dL/dv0, dL/dq, dL/dm)."""
+    pos = np.ascontiguousarray(pos, np.float64).reshape(-1)
+    n = pos.shape[0] // 3
+    gx0, gv0, gq, gm = np.zeros(3 * n), np.zeros(3 * n), np.zeros(n), np.zeros(n)
+    lib().orc_leapfrog_adjoint(n, pos, np.ascontiguousarray(vel, np.float64).reshape(-1),
+                               np.ascontiguousarray(q, np.float64), np.ascontiguousarray(m, np.float64), eps, G, dt,
+                               steps, np.ascontiguousarray(gxT, np.float64).reshape(-1),
+                               np.ascontiguousarray(gvT, np.float64).reshape(-1), gx0, gv0, gq, gm,
+                               nthreads or min(os.cpu_count() or 1, 32))
+    return gx0.reshape(-1, 3), gv0.reshape(-1, 3), gq, gm
 
 
 def naive_steps(pos4, vel4, mass, charge, G, dt, steps, fix_delta=False):

@@ -221,3 +221,78 @@ def test_initial_conditions_are_seeded_and_sane():
     assert abs(mm.sum() - 1) < 1e-12 and p.shape == (4000, 3)
     c = ics.clustered(6400, seed=2)
     assert abs(c[2].sum() - 1) < 1e-12
+
+
+def test_direct_sum_vjp_matches_finite_differences(oracle):
+    """The FP64 adjoint oracle against central differences of the FP64 direct sum."""
+    rng = np.random.default_rng(11)
+    n = 150
+    pos = rng.normal(size=(n, 3))
+    q = rng.uniform(0.5, 1.5, n)
+    m = rng.uniform(0.5, 1.5, n)
+    mu = rng.normal(size=(n, 3))
+    gx, gq, gm = oracle.direct_vjp(pos, q, m, mu, eps=0.05, G=0.7)
+
+    def S(p=pos, qq=q, mm=m):
+        a, _ = oracle.direct(p, qq, mm, eps=0.05, G=0.7)
+        return float(np.sum(mu * a))
+
+    for k in (0, 17, 149):
+        for d in range(3):
+            e = np.zeros_like(pos)
+            e[k, d] = 1e-6
+            fd = (S(p=pos + e) - S(p=pos - e)) / 2e-6
+            assert abs(fd - gx[k, d]) < 1e-6 * max(1.0, abs(gx[k, d]))
+        e = np.zeros(n)
+        e[k] = 1e-6
+        assert abs((S(qq=q + e) - S(qq=q - e)) / 2e-6 - gq[k]) < 1e-6 * max(1.0, abs(gq[k]))
+        assert abs((S(mm=m + e) - S(mm=m - e)) / 2e-6 - gm[k]) < 1e-6 * max(1.0, abs(gm[k]))
+
+
+def test_leapfrog_adjoint_matches_finite_differences(oracle):
+    """The trajectory adjoint oracle against central differences of the FP64 direct-sum leapfrog."""
+    rng = np.random.default_rng(12)
+    n, steps, dt, eps = 40, 4, 0.01, 0.05
+    pos, vel = rng.normal(size=(n, 3)), 0.3 * rng.normal(size=(n, 3))
+    q = m = rng.uniform(0.5, 1.5, n) / n
+    wx, wv = rng.normal(size=(n, 3)), rng.normal(size=(n, 3))
+    gx0, gv0, gq, gm = oracle.leapfrog_adjoint(pos, vel, q, m, eps, 1.0, dt, steps, wx, wv)
+
+    def L(p=pos, v=vel, qq=q, mm=m):
+        p1, v1, _ = oracle.leapfrog(p, v, qq, mm, eps, 1.0, dt, steps)
+        return float(np.sum(wx * p1) + np.sum(wv * v1))
+
+    h = 1e-6
+    for k in (0, 39):
+        for d in range(3):
+            e = np.zeros_like(pos)
+            e[k, d] = h
+            assert abs((L(p=pos + e) - L(p=pos - e)) / (2 * h) - gx0[k, d]) < 1e-6
+            assert abs((L(v=vel + e) - L(v=vel - e)) / (2 * h) - gv0[k, d]) < 1e-6
+        e = np.zeros(n)
+        e[k] = h
+        fq = (L(qq=q + e, mm=m) - L(qq=q - e, mm=m)) / (2 * h)
+        fm = (L(qq=q, mm=m + e) - L(qq=q, mm=m - e)) / (2 * h)
+        assert abs(fq - gq[k]) < 1e-5 * max(1.0, abs(gq[k]))
+        assert abs(fm - gm[k]) < 1e-5 * max(1.0, abs(gm[k]))
+
+
+def test_frozen_tree_fmm_derivative_approaches_direct_vjp(oracle):
+    """Finite differences of the oracle FMM with its tree frozen converge to the direct-sum VJP with order."""
+    pos, vel, m = ics.plummer(1500, seed=13)
+    rng = np.random.default_rng(13)
+    mu, d = rng.normal(size=pos.shape), rng.normal(size=pos.shape)
+    gx, _, _ = oracle.direct_vjp(pos, m, m, mu, eps=0.01)
+    exact = float(np.sum(gx * d))
+    t = oracle.Tree(pos, m, m, cap=16).traverse(0.5)
+    errs = []
+    for p in (1, 4, 8):
+        def S(x):
+            t.set_particles(pos=x)
+            a, _ = t.fmm(p, 0.01)
+            return float(np.sum(mu * a))
+        fd = (S(pos + 1e-6 * d) - S(pos - 1e-6 * d)) / 2e-6
+        errs.append(abs(fd - exact) / abs(exact))
+    t.set_particles(pos=pos)
+    assert errs[0] > errs[1] > errs[2]
+    assert errs[2] < 1e-5 and errs[0] < 2e-2
