@@ -9,11 +9,12 @@
 //   its VJP is taken with mu = c lambda_v and added to lambda_x, q and m;
 //   before time point pt < N the drift x_{pt+1} = x_pt + dt v gives
 //   lambda_v += dt lambda_x.
-// Forces at a time point need its tree, lists and local expansions, so each
-// time point is re-evaluated from a snapshot (the run's last point and the last
-// point of every recomputed segment are already current).  Snapshots hold the
-// sorted state (positions, velocities, accelerations, masses, charges, ids), so
-// a recomputed segment is bitwise the recorded one.
+// The VJP at a time point needs its tree, lists and local expansions, so each
+// time point is re-evaluated from a snapshot, far field only: the snapshot
+// already holds that point's accelerations (the run's last point and the last
+// point of every recomputed segment are current without re-evaluation).
+// Snapshots hold the sorted state (positions, velocities, accelerations,
+// masses, charges, ids), so a recomputed segment is bitwise the recorded one.
 #include <algorithm>
 
 #include "nbody_internal.cuh"
@@ -156,6 +157,8 @@ int nbody_force_vjp(nbody_ctx* c, const double* mu, double* gx, double* gq, doub
     NB_TRY(download_r(c, c->adj_gm, n, gm, st + 4 * n));
     NB_CU(c, cudaStreamSynchronize(c->st));
     c->launches = c->launches - l0;
+    if (c->timing)
+        for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&c->phase_ms[7 + i], c->ev[8 + i], c->ev[9 + i]);
     return NBODY_OK;
 }
 
@@ -209,7 +212,7 @@ int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* g
     // time point N
     if (!c->tree_at_final) {
         NB_TRY(snap_load(c, final_slot(c)));
-        NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
+        NB_TRY(nb_evaluate(c, 0, NB_INTEG_FAR_ONLY, false));
     }
     NB_TRY(vjp(c, 0.5 * dt));
     // segments [s0, e), last first
@@ -225,9 +228,9 @@ int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* g
             NB_TRY(rev_drift(c));
             if (pt < e - 1) {
                 NB_TRY(snap_load(c, pt == s0 ? s0 / every : seg_slot(c, pt - s0 - 1)));
-                NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
+                NB_TRY(nb_evaluate(c, 0, NB_INTEG_FAR_ONLY, false));
             } else if (e - 1 == s0) {
-                NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
+                NB_TRY(nb_evaluate(c, 0, NB_INTEG_FAR_ONLY, false));
             }
             NB_TRY(vjp(c, pt == 0 ? 0.5 * dt : dt));
         }

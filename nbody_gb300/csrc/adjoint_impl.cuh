@@ -129,7 +129,8 @@ struct AdjP2PArgs {
     const uint32_t* work_off;
     int64_t nwork;
     const uint32_t* part_off;
-    void* part;               // R[4] per (chunk, target)
+    void* part;               // R[4] per (chunk, target) of multi-chunk leaves
+    void* near;               // R[4] per particle (sorted) of single-chunk leaves
     const uint32_t* ids;
     void *gx, *gq;            // R* accumulators (input order)
     double eps2;
@@ -160,19 +161,165 @@ __device__ __forceinline__ void adj_epilogue(const AdjP2PArgs& A, uint32_t i, co
 
 constexpr int ADJ_WARPS = 4;
 
-template <int MODE, int P>
-__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_p2p(AdjP2PArgs A) {
+// One warp's share of an adjoint near-field work item: every target of the
+// leaf (two per lane, CT lanes per group) against the partner leaves
+// [s_lo, s_hi) of its list.  Per target k the pair sums are kept as
+//   U = sum nu_l / s^3/2,  V = sum q_l / s^3/2,  W = sum r (r . w) / s^5/2,
+//   gq = -sum (nu_l . r) / s^3/2   (r = x_l - x_k, w = q_k nu_l - q_l nu_k)
+// and gx_k = q_k U - V nu_k - 3 W; the self pair is skipped.
+template <int MODE, bool GUARD>
+__device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE>::S4 (*tx)[P2P_TILE],
+                                         typename Prec<MODE>::S4 (*tn)[P2P_TILE], uint32_t k, const NodeRec& nt,
+                                         int64_t li, uint32_t chunk, uint32_t nchunk, uint32_t s_lo, uint32_t s_hi) {
     typedef typename Prec<MODE>::R R;
     typedef typename Prec<MODE>::S S;
-    typedef typename Prec<MODE>::H H;
     typedef typename Prec<MODE>::S4 S4;
-    constexpr int T = nb_terms<P>::value;
     constexpr bool KH = Prec<MODE>::kahan;
+    const int lane = lane_id();
+    const double unit = A.box->unit;
+    const S4* src = (const S4*)A.src;
+    const S4* nu = (const S4*)A.nu;
+    const uint32_t cnt_t = nt.count;
+    const int CT = cnt_t <= 16 ? 8 : cnt_t <= 32 ? 16 : 32;
+    const int NG = 32 / CT, grp = lane / CT, gl = lane % CT;
+    const uint32_t loff = A.p2p_off[k];
+    const S eps2 = (S)A.eps2;
+    S4 zero4;
+    zero4.x = 0; zero4.y = 0; zero4.z = 0; zero4.w = 0;
+    for (uint32_t tc = 0; tc < cnt_t; tc += 2 * CT) {
+        const uint32_t ta = tc + gl, tb = tc + CT + gl;
+        const bool va = ta < cnt_t, vb = tb < cnt_t;
+        const uint32_t ia = nt.begin + (va ? ta : 0), ib = nt.begin + (vb ? tb : 0);
+        const S4 ya = src[ia], yb = src[ib], na = nu[ia], nb = nu[ib];
+        // sums: U (3), V, W (3), gq per target, with compensation terms
+        S sa[8], sb_[8], ca[8], cb[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) { sa[j] = 0; sb_[j] = 0; ca[j] = 0; cb[j] = 0; }
+        for (uint32_t base = s_lo; base < s_hi; base += 32) {
+            const uint32_t nbat = min(32u, s_hi - base);
+            uint32_t my_s = 0, my_beg = 0, my_cnt = 0;
+            S my_dx = 0, my_dy = 0, my_dz = 0;
+            if ((uint32_t)lane < nbat) {
+                my_s = A.p2p_list[loff + base + lane];
+                const NodeRec sn = A.nodes[my_s];
+                my_beg = sn.begin;
+                my_cnt = sn.count;
+                double ddx, ddy, ddz;
+                disp(sn, nt, unit, ddx, ddy, ddz);
+                my_dx = (S)ddx; my_dy = (S)ddy; my_dz = (S)ddz;
+            }
+            // partners of this batch in descending particle count: the NG groups of a round then
+            // take leaves of similar size, so fewer lanes wait on the longest one
+            {
+                const uint32_t key = (min(my_cnt, 1u << 26) << 5) | (31u - (uint32_t)lane);
+                const int from = 31 - (int)(warp_sort_desc(key) & 31u);
+                my_s = __shfl_sync(0xffffffffu, my_s, from);
+                my_beg = __shfl_sync(0xffffffffu, my_beg, from);
+                my_cnt = __shfl_sync(0xffffffffu, my_cnt, from);
+                my_dx = __shfl_sync(0xffffffffu, my_dx, from);
+                my_dy = __shfl_sync(0xffffffffu, my_dy, from);
+                my_dz = __shfl_sync(0xffffffffu, my_dz, from);
+            }
+            const uint32_t rounds = (nbat + NG - 1) / NG;
+            for (uint32_t rr = 0; rr < rounds; ++rr) {
+                const uint32_t q = rr * NG + grp;
+                const uint32_t qs = q & 31;
+                const uint32_t s_id = __shfl_sync(0xffffffffu, my_s, qs);
+                const uint32_t beg = __shfl_sync(0xffffffffu, my_beg, qs);
+                const uint32_t scnt0 = __shfl_sync(0xffffffffu, my_cnt, qs);
+                const S dx = __shfl_sync(0xffffffffu, my_dx, qs), dy = __shfl_sync(0xffffffffu, my_dy, qs),
+                        dz = __shfl_sync(0xffffffffu, my_dz, qs);
+                const uint32_t scnt = q < nbat ? scnt0 : 0u;
+                uint32_t mx = scnt;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                const bool self = s_id == k && q < nbat;
+                const S xa = ya.x - dx, ya_ = ya.y - dy, za = ya.z - dz;
+                const S xb = yb.x - dx, yb_ = yb.y - dy, zb = yb.z - dz;
+                for (uint32_t t0 = 0; t0 < mx; t0 += P2P_TILE) {
+                    for (int e = gl; e < P2P_TILE; e += CT) {
+                        const uint32_t j = t0 + e;
+                        tx[grp][e] = j < scnt ? src[beg + j] : zero4;
+                        tn[grp][e] = j < scnt ? nu[beg + j] : zero4;
+                    }
+                    __syncwarp();
+                    const int nj = scnt > t0 ? min((int)(scnt - t0), P2P_TILE) : 0;
+                    const int selfa = self ? (int)ta - (int)t0 : -1, selfb = self ? (int)tb - (int)t0 : -1;
+                    S pa[8], pb[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) { pa[j] = 0; pb[j] = 0; }
+#pragma unroll 1
+                    for (int e = 0; e < nj; ++e) {
+                        const S4 sx = tx[grp][e], sv = tn[grp][e];
+                        {
+                            const S rx = sx.x - xa, ry = sx.y - ya_, rz = sx.z - za;
+                            S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
+                            if (GUARD) s2 = s2 > S(0) ? s2 : S(1e30);
+                            S inv = nb_rsqrt(s2);
+                            if (e == selfa) inv = S(0);
+                            const S inv2 = inv * inv, inv3 = inv2 * inv, inv5 = inv3 * inv2;
+                            const S dl = nb_fma(sv.x, rx, nb_fma(sv.y, ry, sv.z * rz));
+                            const S dk = nb_fma(na.x, rx, nb_fma(na.y, ry, na.z * rz));
+                            const S t = nb_fma(ya.w, dl, -sx.w * dk) * inv5;
+                            pa[0] = nb_fma(sv.x, inv3, pa[0]); pa[1] = nb_fma(sv.y, inv3, pa[1]);
+                            pa[2] = nb_fma(sv.z, inv3, pa[2]); pa[3] = nb_fma(sx.w, inv3, pa[3]);
+                            pa[4] = nb_fma(rx, t, pa[4]); pa[5] = nb_fma(ry, t, pa[5]); pa[6] = nb_fma(rz, t, pa[6]);
+                            pa[7] = nb_fma(dl, inv3, pa[7]);
+                        }
+                        {
+                            const S rx = sx.x - xb, ry = sx.y - yb_, rz = sx.z - zb;
+                            S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
+                            if (GUARD) s2 = s2 > S(0) ? s2 : S(1e30);
+                            S inv = nb_rsqrt(s2);
+                            if (e == selfb) inv = S(0);
+                            const S inv2 = inv * inv, inv3 = inv2 * inv, inv5 = inv3 * inv2;
+                            const S dl = nb_fma(sv.x, rx, nb_fma(sv.y, ry, sv.z * rz));
+                            const S dk = nb_fma(nb.x, rx, nb_fma(nb.y, ry, nb.z * rz));
+                            const S t = nb_fma(yb.w, dl, -sx.w * dk) * inv5;
+                            pb[0] = nb_fma(sv.x, inv3, pb[0]); pb[1] = nb_fma(sv.y, inv3, pb[1]);
+                            pb[2] = nb_fma(sv.z, inv3, pb[2]); pb[3] = nb_fma(sx.w, inv3, pb[3]);
+                            pb[4] = nb_fma(rx, t, pb[4]); pb[5] = nb_fma(ry, t, pb[5]); pb[6] = nb_fma(rz, t, pb[6]);
+                            pb[7] = nb_fma(dl, inv3, pb[7]);
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        if (KH) { kahan_add(sa[j], ca[j], pa[j]); kahan_add(sb_[j], cb[j], pb[j]); }
+                        else { sa[j] += pa[j]; sb_[j] += pb[j]; }
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+        // combine the source groups in a fixed order, in the state precision
+        R ra[8], rb[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) { ra[j] = (R)sa[j] - (R)ca[j]; rb[j] = (R)sb_[j] - (R)cb[j]; }
+        for (int o = CT; o < 32; o <<= 1) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) { ra[j] += shfl_xor_t(ra[j], o); rb[j] += shfl_xor_t(rb[j], o); }
+        }
+        if (grp == 0) {
+            const R qa = (R)ya.w, qb = (R)yb.w;
+            const R ga[4] = {qa * ra[0] - ra[3] * (R)na.x - R(3) * ra[4], qa * ra[1] - ra[3] * (R)na.y - R(3) * ra[5],
+                             qa * ra[2] - ra[3] * (R)na.z - R(3) * ra[6], -ra[7]};
+            const R gb[4] = {qb * rb[0] - rb[3] * (R)nb.x - R(3) * rb[4], qb * rb[1] - rb[3] * (R)nb.y - R(3) * rb[5],
+                             qb * rb[2] - rb[3] * (R)nb.z - R(3) * rb[6], -rb[7]};
+            R* pt = nchunk == 1 ? (R*)A.near + 4 * (int64_t)nt.begin
+                                : (R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)chunk * cnt_t);
+            if (va) { pt[4 * ta] = ga[0]; pt[4 * ta + 1] = ga[1]; pt[4 * ta + 2] = ga[2]; pt[4 * ta + 3] = ga[3]; }
+            if (vb) { pt[4 * tb] = gb[0]; pt[4 * tb + 1] = gb[1]; pt[4 * tb + 2] = gb[2]; pt[4 * tb + 3] = gb[3]; }
+        }
+        __syncwarp();
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_p2p(AdjP2PArgs A) {
+    typedef typename Prec<MODE>::S4 S4;
     __shared__ S4 tx[ADJ_WARPS][4][P2P_TILE];
     __shared__ S4 tn[ADJ_WARPS][4][P2P_TILE];
-    __shared__ S sL[ADJ_WARPS][T];
-    __shared__ S sM[ADJ_WARPS][T];
-    const int lane = lane_id(), wib = threadIdx.x >> 5;
+    const int wib = threadIdx.x >> 5;
     const int64_t w = (int64_t)blockIdx.x * ADJ_WARPS + wib;
     if (w >= A.nwork) return;
     int64_t lo = 0, hi = A.nleaves;
@@ -185,109 +332,16 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_p2p(AdjP2PArgs A) {
     const uint32_t nchunk = A.work_off[li + 1] - A.work_off[li];
     const uint32_t k = A.leaves[li];
     const NodeRec nt = A.nodes[k];
-    const double unit = A.box->unit;
-    const S4* src = (const S4*)A.src;
-    const S4* nu = (const S4*)A.nu;
-    if (nchunk == 1) {
-        const H* Lg = (const H*)A.L;
-        const H* Mg = (const H*)A.lamM;
-        for (int a = lane; a < T; a += 32) {
-            sL[wib][a] = (S)Lg[(int64_t)k * T + a];
-            sM[wib][a] = (S)Mg[(int64_t)k * T + a];
-        }
-    }
-    const uint32_t cnt_t = nt.count;
-    const int CT = cnt_t <= 8 ? 8 : cnt_t <= 16 ? 16 : 32;
-    const int NG = 32 / CT, grp = lane / CT, gl = lane % CT;
-    const uint32_t loff = A.p2p_off[k], lcnt = A.p2p_cnt[k];
+    const uint32_t lcnt = A.p2p_cnt[k];
     const uint32_t s_lo = chunk * P2P_CHUNK, s_hi = min(lcnt, s_lo + P2P_CHUNK);
-    const S eps2 = (S)A.eps2;
-    const bool guard = !(A.eps2 > 0.0);
-    __syncwarp();
-    for (uint32_t tc = 0; tc < cnt_t; tc += CT) {
-        const uint32_t ti = tc + gl;
-        const bool tv = ti < cnt_t;
-        const uint32_t i = nt.begin + (tv ? ti : 0);
-        const S4 yk = src[i], nk = nu[i];
-        S gx = 0, gy = 0, gz = 0, gq = 0, cx = 0, cy = 0, cz = 0, cq = 0;
-        for (uint32_t base = s_lo; base < s_hi; base += 32) {
-            const uint32_t nb = min(32u, s_hi - base);
-            uint32_t my_beg = 0, my_cnt = 0;
-            S my_dx = 0, my_dy = 0, my_dz = 0;
-            if ((uint32_t)lane < nb) {
-                const NodeRec sn = A.nodes[A.p2p_list[loff + base + lane]];
-                my_beg = sn.begin;
-                my_cnt = sn.count;
-                double ddx, ddy, ddz;
-                disp(sn, nt, unit, ddx, ddy, ddz);
-                my_dx = (S)ddx; my_dy = (S)ddy; my_dz = (S)ddz;
-            }
-            const uint32_t rounds = (nb + NG - 1) / NG;
-            for (uint32_t rr = 0; rr < rounds; ++rr) {
-                const uint32_t q = rr * NG + grp;
-                const uint32_t qs = q & 31;
-                const uint32_t beg = __shfl_sync(0xffffffffu, my_beg, qs);
-                const uint32_t scnt0 = __shfl_sync(0xffffffffu, my_cnt, qs);
-                const S dx = __shfl_sync(0xffffffffu, my_dx, qs), dy = __shfl_sync(0xffffffffu, my_dy, qs),
-                        dz = __shfl_sync(0xffffffffu, my_dz, qs);
-                const uint32_t scnt = q < nb ? scnt0 : 0u;
-                uint32_t mx = scnt;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-                const S xk = yk.x - dx, yk_ = yk.y - dy, zk = yk.z - dz;
-                for (uint32_t sb = 0; sb < mx; sb += P2P_TILE) {
-                    for (int e = gl; e < P2P_TILE; e += CT) {
-                        const uint32_t j = sb + e;
-                        S4 a, b;
-                        if (j < scnt) { a = src[beg + j]; b = nu[beg + j]; }
-                        else { a.x = 0; a.y = 0; a.z = 0; a.w = 0; b = a; }
-                        tx[wib][grp][e] = a;
-                        tn[wib][grp][e] = b;
-                    }
-                    __syncwarp();
-                    const int nj = scnt > sb ? min((int)(scnt - sb), P2P_TILE) : 0;
-                    S px = 0, py = 0, pz = 0, pq = 0;
-                    for (int e = 0; e < nj; ++e) {
-                        const S4 sx = tx[wib][grp][e], sv = tn[wib][grp][e];
-                        const S rx = sx.x - xk, ry = sx.y - yk_, rz = sx.z - zk;
-                        S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
-                        if (guard) s2 = s2 > S(0) ? s2 : S(1e30);
-                        const S inv = nb_rsqrt(s2), inv2 = inv * inv, inv3 = inv2 * inv, inv5 = inv3 * inv2;
-                        const S wx = yk.w * sv.x - sx.w * nk.x, wy = yk.w * sv.y - sx.w * nk.y,
-                                wz = yk.w * sv.z - sx.w * nk.z;
-                        const S t3 = S(3) * nb_fma(rx, wx, nb_fma(ry, wy, rz * wz)) * inv5;
-                        px = nb_fma(wx, inv3, nb_fma(-rx, t3, px));
-                        py = nb_fma(wy, inv3, nb_fma(-ry, t3, py));
-                        pz = nb_fma(wz, inv3, nb_fma(-rz, t3, pz));
-                        pq = nb_fma(-nb_fma(sv.x, rx, nb_fma(sv.y, ry, sv.z * rz)), inv3, pq);
-                    }
-                    if (KH) {
-                        kahan_add(gx, cx, px); kahan_add(gy, cy, py); kahan_add(gz, cz, pz); kahan_add(gq, cq, pq);
-                    } else {
-                        gx += px; gy += py; gz += pz; gq += pq;
-                    }
-                    __syncwarp();
-                }
-            }
-        }
-        R Gx = (R)gx - (R)cx, Gy = (R)gy - (R)cy, Gz = (R)gz - (R)cz, Gq = (R)gq - (R)cq;
-        for (int o = CT; o < 32; o <<= 1) {
-            Gx += shfl_xor_t(Gx, o); Gy += shfl_xor_t(Gy, o); Gz += shfl_xor_t(Gz, o); Gq += shfl_xor_t(Gq, o);
-        }
-        if (grp == 0 && tv) {
-            if (nchunk == 1) {
-                adj_epilogue<MODE, P>(A, i, sL[wib], sM[wib], yk, nk, Gx, Gy, Gz, Gq);
-            } else {
-                R* pt = (R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)chunk * cnt_t + ti);
-                pt[0] = Gx; pt[1] = Gy; pt[2] = Gz; pt[3] = Gq;
-            }
-        }
-        __syncwarp();
-    }
+    if (A.eps2 > 0.0) adj_item<MODE, false>(A, tx[wib], tn[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
+    else adj_item<MODE, true>(A, tx[wib], tn[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
 }
 
+// near-field sums of every particle (chunk partials added in chunk order), then the far-field
+// adjoint terms and the input-order accumulation; a warp per leaf
 template <int MODE, int P>
-__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_p2p_final(AdjP2PArgs A) {
+__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_finish(AdjP2PArgs A) {
     typedef typename Prec<MODE>::R R;
     typedef typename Prec<MODE>::S S;
     typedef typename Prec<MODE>::H H;
@@ -299,7 +353,6 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_p2p_final(AdjP2PArgs A) 
     const int64_t li = (int64_t)blockIdx.x * ADJ_WARPS + wib;
     if (li >= A.nleaves) return;
     const uint32_t nchunk = A.work_off[li + 1] - A.work_off[li];
-    if (nchunk <= 1) return;
     const uint32_t k = A.leaves[li];
     const NodeRec nt = A.nodes[k];
     const H* Lg = (const H*)A.L;
@@ -312,12 +365,17 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_p2p_final(AdjP2PArgs A) 
     const S4* src = (const S4*)A.src;
     const S4* nu = (const S4*)A.nu;
     for (uint32_t ti = lane; ti < nt.count; ti += 32) {
-        R e[4] = {0, 0, 0, 0};
-        for (uint32_t c = 0; c < nchunk; ++c) {
-            const R* pt = (const R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)c * nt.count + ti);
-            e[0] += pt[0]; e[1] += pt[1]; e[2] += pt[2]; e[3] += pt[3];
-        }
         const uint32_t i = nt.begin + ti;
+        R e[4] = {0, 0, 0, 0};
+        if (nchunk == 1) {
+            const R* pt = (const R*)A.near + 4 * (int64_t)i;
+            e[0] = pt[0]; e[1] = pt[1]; e[2] = pt[2]; e[3] = pt[3];
+        } else {
+            for (uint32_t c = 0; c < nchunk; ++c) {
+                const R* pt = (const R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)c * nt.count + ti);
+                e[0] += pt[0]; e[1] += pt[1]; e[2] += pt[2]; e[3] += pt[3];
+            }
+        }
         adj_epilogue<MODE, P>(A, i, sL[wib], sM[wib], src[i], nu[i], e[0], e[1], e[2], e[3]);
     }
 }
@@ -348,6 +406,7 @@ int force_vjp(nbody_ctx* c, double coef) {
     A.G = c->prm.G;
     A.nu = c->adj_nu.p;
     A.gx = c->adj_lx.p; A.gq = c->adj_gq.p; A.gm = c->adj_gm.p;
+    if (c->timing) cudaEventRecord(c->ev[8], c->st);
     k_adj_prep<MODE><<<(unsigned)((n + 255) / 256), 256, 0, c->st>>>(A);
     NB_LAUNCHED(c, "adj_prep");
     c->launches += 1;
@@ -356,6 +415,7 @@ int force_vjp(nbody_ctx* c, double coef) {
         lamL32);
     NB_LAUNCHED(c, "adj_l2pT");
     c->launches += 1;
+    if (c->timing) cudaEventRecord(c->ev[9], c->st);
     for (int l = c->depth - 1; l >= 0; --l) {
         const int lo = c->level_start[l], hi = c->level_start[l + 1];
         if (hi <= lo) continue;
@@ -364,6 +424,7 @@ int force_vjp(nbody_ctx* c, double coef) {
         NB_LAUNCHED(c, "adj_l2lT");
         c->launches += 1;
     }
+    if (c->timing) cudaEventRecord(c->ev[10], c->st);
     {
         M2LArgs B;
         B.nodes = DP<NodeRec>(c->nodes);
@@ -382,6 +443,7 @@ int force_vjp(nbody_ctx* c, double coef) {
         NB_LAUNCHED(c, "adj_m2lT");
         c->launches += 1;
     }
+    if (c->timing) cudaEventRecord(c->ev[11], c->st);
     for (int r = 1; r <= c->depth; ++r) {
         const int lo = c->level_start[r], hi = c->level_start[r + 1];
         if (hi <= lo) continue;
@@ -390,6 +452,7 @@ int force_vjp(nbody_ctx* c, double coef) {
         NB_LAUNCHED(c, "adj_m2mT");
         c->launches += 1;
     }
+    if (c->timing) cudaEventRecord(c->ev[12], c->st);
     AdjP2PArgs C;
     C.leaves = DP<uint32_t>(c->leaves);
     C.nleaves = nl;
@@ -404,16 +467,18 @@ int force_vjp(nbody_ctx* c, double coef) {
     C.nwork = (uint32_t)c->h_info[INFO_P2P_WORK];
     C.part_off = DP<uint32_t>(c->p2p_part_off);
     C.part = c->p2p_part.p;
+    NB_TRY(nb_grow(c, c->adj_near, 4 * sizeof(R) * (size_t)n));
+    C.near = c->adj_near.p;
     C.ids = DP<uint32_t>(c->id[cur]);
     C.gx = c->adj_lx.p;
     C.gq = c->adj_gq.p;
     C.eps2 = c->prm.eps * c->prm.eps;
-    const int64_t npart = (uint32_t)c->h_info[INFO_P2P_PART];
-    k_adj_p2p<MODE, P><<<(unsigned)((C.nwork + ADJ_WARPS - 1) / ADJ_WARPS), 32 * ADJ_WARPS, 0, c->st>>>(C);
-    if (npart)
-        k_adj_p2p_final<MODE, P><<<(unsigned)((nl + ADJ_WARPS - 1) / ADJ_WARPS), 32 * ADJ_WARPS, 0, c->st>>>(C);
+    k_adj_p2p<MODE><<<(unsigned)((C.nwork + ADJ_WARPS - 1) / ADJ_WARPS), 32 * ADJ_WARPS, 0, c->st>>>(C);
     NB_LAUNCHED(c, "adj_p2p");
-    c->launches += npart ? 2 : 1;
+    k_adj_finish<MODE, P><<<(unsigned)((nl + ADJ_WARPS - 1) / ADJ_WARPS), 32 * ADJ_WARPS, 0, c->st>>>(C);
+    NB_LAUNCHED(c, "adj_finish");
+    c->launches += 2;
+    if (c->timing) cudaEventRecord(c->ev[13], c->st);
     return NBODY_OK;
 }
 

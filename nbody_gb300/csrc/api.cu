@@ -269,7 +269,7 @@ int nbody_create(const nbody_params* p, nbody_ctx** out) {
         if ((rc = nb_grow(c, c->bbox, 6 * sizeof(unsigned long long)))) break;
         if ((rc = nb_cuda(c, cudaMallocHost(&c->h_info, sizeof(int32_t) * INFO_WORDS), "cudaMallocHost"))) break;
         if ((rc = nb_cuda(c, cudaMemsetAsync(c->info.p, 0, sizeof(int32_t) * INFO_WORDS, c->st), "memset"))) break;
-        for (int i = 0; i < 8 && !rc; ++i) rc = nb_cuda(c, cudaEventCreate(&c->ev[i]), "cudaEventCreate");
+        for (int i = 0; i < 14 && !rc; ++i) rc = nb_cuda(c, cudaEventCreate(&c->ev[i]), "cudaEventCreate");
     } while (0);
     if (rc) {
         g_create_err = c->err;
@@ -293,7 +293,8 @@ int nbody_destroy(nbody_ctx* c) {
                       &c->nodes, &c->leafflag, &c->leafpfx, &c->leaves, &c->M, &c->M32, &c->L, &c->src, &c->pend_off,
                       &c->pend_cnt, &c->p2p_off, &c->p2p_cnt, &c->pend_list, &c->p2p_list, &c->m2l_off, &c->m2l_cnt,
                       &c->m2l_list, &c->stage, &c->diag, &c->info, &c->box, &c->bbox, &c->adj_lx, &c->adj_lv,
-                      &c->adj_gq, &c->adj_gm, &c->adj_nu, &c->adj_lamL, &c->adj_lamL32, &c->adj_lamM, &c->snaps})
+                      &c->adj_gq, &c->adj_gm, &c->adj_nu, &c->adj_lamL, &c->adj_lamL32, &c->adj_lamM, &c->adj_near,
+                      &c->snaps})
         release(*b);
     if (c->h_info) cudaFreeHost(c->h_info);
     for (int i = 0; i < 16; ++i)
@@ -498,7 +499,7 @@ int nbody_set_timing(nbody_ctx* c, int on) {
 
 int nbody_phase_times(nbody_ctx* c, float* ms, int n) {
     if (!c || !ms) return NBODY_ERR_INVALID;
-    for (int i = 0; i < n && i < 7; ++i) ms[i] = c->phase_ms[i];
+    for (int i = 0; i < n && i < 12; ++i) ms[i] = c->phase_ms[i];
     return NBODY_OK;
 }
 

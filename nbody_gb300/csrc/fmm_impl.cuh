@@ -789,6 +789,18 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
                 disp(sn, nt, unit, ddx, ddy, ddz);
                 my_dx = (S)ddx; my_dy = (S)ddy; my_dz = (S)ddz;
             }
+            // partners of this batch in descending particle count: the NG groups of a round then
+            // take leaves of similar size, so fewer lanes wait on the longest one
+            {
+                const uint32_t key = (min(my_cnt, 1u << 26) << 5) | (31u - (uint32_t)lane);
+                const int from = 31 - (int)(warp_sort_desc(key) & 31u);
+                my_s = __shfl_sync(0xffffffffu, my_s, from);
+                my_beg = __shfl_sync(0xffffffffu, my_beg, from);
+                my_cnt = __shfl_sync(0xffffffffu, my_cnt, from);
+                my_dx = __shfl_sync(0xffffffffu, my_dx, from);
+                my_dy = __shfl_sync(0xffffffffu, my_dy, from);
+                my_dz = __shfl_sync(0xffffffffu, my_dz, from);
+            }
             const uint32_t rounds = (nb + NG - 1) / NG;
             uint32_t rr = 0, sb = 0;
             const uint32_t cur_beg = __shfl_sync(0xffffffffu, my_beg, grp);
@@ -1096,6 +1108,10 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     }
     if (c->timing) cudaEventRecord(c->ev[6], c->st);
 
+    if (integ == NB_INTEG_FAR_ONLY) {
+        if (c->timing) cudaEventRecord(c->ev[7], c->st);
+        return NBODY_OK;
+    }
     const int64_t nl = c->nleaves;
     const int64_t nwork = (uint32_t)c->h_info[INFO_P2P_WORK];
     const int64_t npart = (uint32_t)c->h_info[INFO_P2P_PART];

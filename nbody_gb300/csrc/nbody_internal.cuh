@@ -102,7 +102,7 @@ struct nbody_ctx {
     double* h_box = nullptr;
 
     // adjoint (input-order accumulators, adjoint expansions, trajectory snapshots)
-    DevBuf adj_lx, adj_lv, adj_gq, adj_gm, adj_nu, adj_lamL, adj_lamL32, adj_lamM;
+    DevBuf adj_lx, adj_lv, adj_gq, adj_gm, adj_nu, adj_lamL, adj_lamL32, adj_lamM, adj_near;
     DevBuf snaps;                  // sorted-state snapshots: checkpoints, segment scratch, final state
     size_t snap_bytes = 0;         // bytes of one snapshot
     int ck_steps = 0;              // steps of the recorded run (0: nothing recorded)
@@ -112,7 +112,7 @@ struct nbody_ctx {
 
     // per-phase timing
     bool timing = false;
-    cudaEvent_t ev[16] = {};
+    cudaEvent_t ev[16] = {};       // 0..7 force evaluation, 8..13 force VJP
     float phase_ms[16] = {0};
 
     std::string err;
@@ -159,7 +159,8 @@ int nb_fmm_vjp_mixed(nbody_ctx* c, double coef);
 int nb_fmm_vjp_fp64(nbody_ctx* c, double coef);
 
 // integration modes of the force epilogue
-enum { NB_INTEG_NONE = 0, NB_INTEG_KDK_CLOSE = 1, NB_INTEG_EULER = 2 };
+// NB_INTEG_FAR_ONLY: tree, lists and far field only (accelerations already known, e.g. from a snapshot)
+enum { NB_INTEG_NONE = 0, NB_INTEG_KDK_CLOSE = 1, NB_INTEG_EULER = 2, NB_INTEG_FAR_ONLY = 3 };
 
 // ---------------------------------------------------------------------------
 // device helpers
@@ -187,6 +188,21 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
     for (int o = 1; o < 32; o <<= 1) {
         uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
         if (lane_id() >= (uint32_t)o) v += t;
+    }
+    return v;
+}
+
+// bitonic sort of one unique key per lane, descending across the warp
+__device__ __forceinline__ uint32_t warp_sort_desc(uint32_t v) {
+    const uint32_t lane = lane_id();
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const uint32_t o = __shfl_xor_sync(0xffffffffu, v, j);
+            const bool keep_max = ((lane & j) == 0) == ((lane & k) == 0);
+            v = keep_max ? max(v, o) : min(v, o);
+        }
     }
     return v;
 }

@@ -236,11 +236,19 @@ class CudaSimulation:
         check(self._h, _lib.load().nbody_set_timing(self._h, int(on)))
 
     PHASES = ("kick_drift_keys", "sort_gather", "tree", "upward", "lists", "far_field", "near_field")
+    VJP_PHASES = ("adj_seed_l2pT", "adj_l2lT", "adj_m2lT", "adj_m2mT", "adj_near")
 
     def phase_times(self):
-        out = np.zeros(7, np.float32)
-        check(self._h, _lib.load().nbody_phase_times(self._h, ptr(out), 7))
-        return out
+        """Device ms of the last force evaluation's phases (PHASES)."""
+        out = np.zeros(12, np.float32)
+        check(self._h, _lib.load().nbody_phase_times(self._h, ptr(out), 12))
+        return out[:7]
+
+    def vjp_phase_times(self):
+        """Device ms of the last force_vjp's phases (VJP_PHASES)."""
+        out = np.zeros(12, np.float32)
+        check(self._h, _lib.load().nbody_phase_times(self._h, ptr(out), 12))
+        return out[7:]
 
     @property
     def stream(self) -> int:
