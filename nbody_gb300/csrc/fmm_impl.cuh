@@ -8,11 +8,8 @@
 //               particle's offset from its leaf centre (packed with its charge);
 //   k_m2m       one tree level per launch, children shifted to the parent
 //               centre (translation offsets exact, in the shift precision);
-//   k_classify  one tree level per launch: a warp per target cell refines its
-//               parent's pending partners (src/interaction.cl:10-100 MAC and
-//               split rules) into contiguous per-target far-field, near-field
-//               and pending lists; leaf targets descend remaining partners
-//               with a per-warp stack;
+//   (lists.cu)  the far-field and near-field lists of every cell
+//               (src/interaction.cl:10-100 MAC and split rules);
 //   k_m2l       every cell's far-field list at once (M2L into per-lane
 //               partial expansions, fixed-order reduction);
 //   k_l2l       one level per launch, parent's local expansion shifted down;
@@ -58,20 +55,6 @@ template <> struct Prec<NBODY_PREC_FP64> {
     static constexpr bool kahan = false;
     static constexpr bool lane_smem = true;   // per-lane M2L arrays live in shared memory
 };
-
-constexpr int STK = 512;         // descent stack entries per warp
-constexpr int CAND = 256;        // expanded candidates per chunk (32 partners x 8 children)
-constexpr uint32_t NONE = 0xffffffffu;
-
-__device__ __forceinline__ int mac_accept(long long tcx, long long tcy, long long tcz, long long tw,
-                                          const NodeRec& s, double theta2x4) {
-    long long sx, sy, sz;
-    nb_centre_fine(s, sx, sy, sz);
-    long long dx = sx - tcx, dy = sy - tcy, dz = sz - tcz;
-    long long d2 = dx * dx + dy * dy + dz * dz;
-    long long e = tw + nb_width_fine(s);
-    return 3.0 * (double)e * (double)e < theta2x4 * (double)d2;
-}
 
 // exact centre displacement (a - b) in box units
 __device__ __forceinline__ void disp(const NodeRec& a, const NodeRec& b, double unit, double& dx, double& dy,
@@ -227,224 +210,6 @@ __global__ void __launch_bounds__(128) k_m2m(int lo, int hi, const NodeRec* __re
         if (a < T) {
             M[(int64_t)k * TM + a] = acc[j];
             if (M32) M32[(int64_t)k * TM + a] = (float)acc[j];
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
-// far field, part 1: interaction lists, one tree level per launch
-//
-// A warp per target cell t of the level refines the pending partners of its
-// parent (src/interaction.cl:10-100 split rules, reorganised per target):
-// each candidate s is a child of a pending partner, or the partner itself if
-// it is a leaf.  s is accepted for the far field when the MAC holds
-// (src/interaction.cl:64-79), kept as a near-field partner when both are
-// leaves, kept pending when t has children, and otherwise (t a leaf, s not)
-// descended with a per-warp stack.  Two passes: the first counts, one
-// atomicAdd per list reserves a contiguous block per target, the second
-// writes in the same order.
-// ---------------------------------------------------------------------------
-template <int MODE, int P>
-__global__ void k_root(const NodeRec* __restrict__ nodes, uint32_t* pend_off, uint32_t* pend_cnt,
-                       uint32_t* pend_list, uint32_t* p2p_off, uint32_t* p2p_cnt, uint32_t* p2p_list,
-                       uint32_t* m2l_off, uint32_t* m2l_cnt, int32_t* info) {
-    if (threadIdx.x == 0) {
-        const bool leaf = nodes[0].nchild == 0;
-        uint32_t* tail = (uint32_t*)&info[leaf ? INFO_P2P_TAIL : INFO_PEND_TAIL];
-        uint32_t o = *tail;
-        *tail = o + 1;
-        if (leaf) { p2p_list[o] = 0; p2p_off[0] = o; p2p_cnt[0] = 1; pend_cnt[0] = 0; }
-        else { pend_list[o] = 0; pend_off[0] = o; pend_cnt[0] = 1; p2p_cnt[0] = 0; }
-        m2l_off[0] = 0;
-        m2l_cnt[0] = 0;
-    }
-}
-
-struct ClassArgs {
-    const NodeRec* nodes;
-    uint32_t *pend_off, *pend_cnt, *pend_list, *p2p_off, *p2p_cnt, *p2p_list, *m2l_off, *m2l_cnt, *m2l_list;
-    uint32_t pend_cap, p2p_cap, m2l_cap;
-    unsigned long long* stats;   // [0] M2L pairs, [1] P2P particle pairs, [2] P2P leaf pairs
-    int32_t* info;
-    float theta2;                // theta^2 formed in FP32, as the reference does
-    int lo, hi;                  // target node range (one level)
-};
-
-// centre (2i+1) << (21 - level) in fine units (side / 2^22); fits in 32 bits
-__device__ __forceinline__ void centre_fine32(const NodeRec& nd, int& cx, int& cy, int& cz) {
-    const int sh = NB_LEVELS - nd.level;
-    cx = (int)((2u * nd.ix + 1u) << sh);
-    cy = (int)((2u * nd.iy + 1u) << sh);
-    cz = (int)((2u * nd.iz + 1u) << sh);
-}
-
-// MAC of src/interaction.cl:64-79 in its own FP32 operation order: displacement of centres,
-// distance^2 = ((x*x + y*y) + z*z) + w*w with w = 0, extent^2 = (0.75 * (wA+wB)) * (wA+wB),
-// approximate iff extent^2 / distance^2 < theta^2 (correctly rounded division).  Lengths are in
-// fine units, an exact power-of-two rescaling of the reference's box units, so every rounding is
-// the reference's.  The division is only evaluated when a cheap estimate is within 0.1 % of the
-// threshold, where it could matter; elsewhere the estimate decides the same way.
-__device__ __forceinline__ bool mac_f32(int tcx, int tcy, int tcz, float tw, const NodeRec& s, float theta2) {
-    int sx, sy, sz;
-    centre_fine32(s, sx, sy, sz);
-    const float dx = (float)(sx - tcx), dy = (float)(sy - tcy), dz = (float)(sz - tcz);
-    const float d2 = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)), 0.0f);
-    const float es = __fadd_rn(tw, (float)(1u << (NB_LEVELS + 1 - s.level)));
-    const float e2 = __fmul_rn(__fmul_rn(0.75f, es), es);
-    const float est = __fdividef(e2, d2);   // within a few ulp of the quotient
-    if (est < 0.999f * theta2) return true;
-    if (est > 1.001f * theta2) return false;
-    return __fdiv_rn(e2, d2) < theta2;
-}
-
-// geometry (level, cell coordinates) of the child in octant oct of a node
-struct CellGeom {
-    uint32_t ix, iy, iz;
-    int level;
-};
-__device__ __forceinline__ CellGeom child_geom(const CellGeom& p, int oct) {
-    return CellGeom{2u * p.ix + (oct & 1), 2u * p.iy + ((oct >> 1) & 1), 2u * p.iz + (oct >> 2), p.level + 1};
-}
-__device__ __forceinline__ void geom_centre(const CellGeom& g, int& cx, int& cy, int& cz) {
-    const int sh = NB_LEVELS - g.level;
-    cx = (int)((2u * g.ix + 1u) << sh);
-    cy = (int)((2u * g.iy + 1u) << sh);
-    cz = (int)((2u * g.iz + 1u) << sh);
-}
-
-constexpr int CLS_WARPS = 8;
-
-static __global__ void __launch_bounds__(32 * CLS_WARPS) k_classify(ClassArgs A) {
-    __shared__ uint32_t s_cand[CLS_WARPS][CAND];
-    __shared__ uint32_t s_stk[CLS_WARPS][STK];
-    const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const int t = A.lo + blockIdx.x * CLS_WARPS + wib;
-    if (t >= A.hi) return;
-    uint32_t* cand = s_cand[wib];
-    uint32_t* stk = s_stk[wib];
-    const NodeRec nt = A.nodes[t];
-    const bool tleaf = nt.nchild == 0;
-    int tcx, tcy, tcz;
-    centre_fine32(nt, tcx, tcy, tcz);
-    const float tw = (float)(1u << (NB_LEVELS + 1 - nt.level));
-    const int par = nt.parent;
-    const uint32_t pb = A.pend_off[par], pc = A.pend_cnt[par];
-    uint32_t* out_list = tleaf ? A.p2p_list : A.pend_list;
-    uint32_t out_base = 0, n_out = 0, m_base = 0, n_apx = 0;
-    bool can_write = false, m_write = false;
-    unsigned long long src_particles = 0;
-
-    for (int pass = 0; pass < 2; ++pass) {
-        uint32_t wpos = 0, mpos = 0;
-        int top = 0;
-        auto classify = [&](uint32_t s) {
-            const bool valid = s != NONE;
-            NodeRec sn;
-            sn.nchild = 0;
-            sn.count = 0;
-            if (valid) sn = A.nodes[s];
-            const bool approx = valid && (int)s != t && mac_f32(tcx, tcy, tcz, tw, sn, A.theta2);
-            const bool sleaf = valid && sn.nchild == 0;
-            const bool out = valid && !approx && (!tleaf || sleaf);
-            const bool desc = valid && !approx && tleaf && !sleaf;
-            const uint32_t mo = __ballot_sync(0xffffffffu, out);
-            if (out && pass == 1 && can_write) {
-                const uint32_t pos = wpos + __popc(mo & lanemask_lt());
-                if (pos < n_out) out_list[out_base + pos] = s;
-                if (tleaf) src_particles += sn.count;
-            }
-            wpos += __popc(mo);
-            const uint32_t ma = __ballot_sync(0xffffffffu, approx);
-            if (approx && pass == 1 && m_write) {
-                const uint32_t pos = mpos + __popc(ma & lanemask_lt());
-                if (pos < n_apx) A.m2l_list[m_base + pos] = s;
-            }
-            mpos += __popc(ma);
-            const uint32_t md = __ballot_sync(0xffffffffu, desc);
-            if (desc) {
-                const int pos = top + __popc(md & lanemask_lt());
-                if (pos < STK) stk[pos] = s;
-                else atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_STACK);
-            }
-            top = min(top + __popc(md), STK);
-        };
-        auto drain_stack = [&]() {
-            while (top > 0) {
-                const int kk = min(top, 4);
-                const int qn = lane >> 3, ci = lane & 7;
-                uint32_t s2 = NONE;
-                if (qn < kk) {
-                    const NodeRec pn = A.nodes[stk[top - 1 - qn]];
-                    if (ci < pn.nchild) s2 = (uint32_t)(pn.child_begin + ci);
-                }
-                __syncwarp();
-                top -= kk;
-                classify(s2);
-                __syncwarp();
-            }
-        };
-        for (uint32_t chunk = 0; chunk < pc; chunk += 32) {
-            const uint32_t j = chunk + lane;
-            uint32_t s = NONE, ns = 0;
-            NodeRec sn;
-            sn.nchild = 0;
-            sn.child_begin = 0;
-            if (j < pc) {
-                s = A.pend_list[pb + j];
-                sn = A.nodes[s];
-                ns = sn.nchild ? sn.nchild : 1u;
-            }
-            const uint32_t inc = warp_incl_scan(ns);
-            const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
-            const uint32_t ex = inc - ns;
-            if (ns == 1 && sn.nchild == 0) cand[ex] = s;
-            else
-                for (uint32_t u = 0; u < ns; ++u) cand[ex + u] = (uint32_t)(sn.child_begin + u);
-            __syncwarp();
-            for (uint32_t g = 0; g < total; g += 32) {
-                const uint32_t s2 = g + lane < total ? cand[g + lane] : NONE;
-                classify(s2);
-            }
-            __syncwarp();
-            drain_stack();
-        }
-        if (pass == 0) {
-            n_out = wpos;
-            n_apx = mpos;
-            uint32_t base = 0, mb = 0;
-            int ok = 0, mok = 0;
-            if (lane == 0) {
-                uint32_t* tail = (uint32_t*)&A.info[tleaf ? INFO_P2P_TAIL : INFO_PEND_TAIL];
-                const uint32_t cap = tleaf ? A.p2p_cap : A.pend_cap;
-                base = atomicAdd(tail, n_out);
-                ok = (uint64_t)base + n_out <= cap;
-                if (!ok) atomicOr((unsigned int*)&A.info[INFO_ERR], tleaf ? NB_ERRBIT_P2P_CAP : NB_ERRBIT_PEND_CAP);
-                mb = atomicAdd((uint32_t*)&A.info[INFO_M2L_TAIL], n_apx);
-                mok = (uint64_t)mb + n_apx <= A.m2l_cap;
-                if (!mok) atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_M2L_CAP);
-                if (tleaf) {
-                    A.p2p_off[t] = base; A.p2p_cnt[t] = ok ? n_out : 0;
-                    A.pend_cnt[t] = 0;
-                } else {
-                    A.pend_off[t] = base; A.pend_cnt[t] = ok ? n_out : 0;
-                    A.p2p_cnt[t] = 0;
-                }
-                A.m2l_off[t] = mb;
-                A.m2l_cnt[t] = mok ? n_apx : 0;
-            }
-            out_base = __shfl_sync(0xffffffffu, base, 0);
-            can_write = __shfl_sync(0xffffffffu, ok, 0);
-            m_base = __shfl_sync(0xffffffffu, mb, 0);
-            m_write = __shfl_sync(0xffffffffu, mok, 0);
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) src_particles += __shfl_xor_sync(0xffffffffu, src_particles, o);
-    if (lane == 0) {
-        atomicAdd(&A.stats[0], (unsigned long long)n_apx);
-        if (tleaf) {
-            atomicAdd(&A.stats[1], src_particles * nt.count);
-            atomicAdd(&A.stats[2], (unsigned long long)n_out);
         }
     }
 }
@@ -701,20 +466,7 @@ __device__ __forceinline__ void kahan_add(S& sum, S& comp, S v) {
 
 constexpr int P2P_WARPS = 4;
 constexpr int P2P_TILE = 32;      // source particles per tile and group
-constexpr int P2P_CHUNK = 256;    // partner leaves per work item
-
-static __global__ void k_p2p_plan(int64_t nleaves, const uint32_t* __restrict__ leaves, const NodeRec* __restrict__ nodes,
-                           const uint32_t* __restrict__ p2p_cnt, uint32_t* __restrict__ nch,
-                           uint32_t* __restrict__ psize) {
-    const int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (li > nleaves) return;
-    if (li == nleaves) { nch[li] = 0; psize[li] = 0; return; }
-    const uint32_t k = leaves[li];
-    const uint32_t c = (p2p_cnt[k] + P2P_CHUNK - 1) / P2P_CHUNK;
-    const uint32_t n = c > 1 ? c : 1u;
-    nch[li] = n;
-    psize[li] = n > 1 ? n * nodes[k].count : 0u;
-}
+constexpr int P2P_CHUNK = NB_P2P_CHUNK;   // partner leaves per work item
 
 template <int MODE, int P>
 __device__ __forceinline__ void p2p_epilogue(const P2PArgs& A, uint32_t i, const typename Prec<MODE>::S* sL,
@@ -977,10 +729,6 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     if (MODE == NBODY_PREC_MIXED) NB_TRY(nb_grow(c, c->M32, sizeof(float) * TM * nn));
     NB_TRY(nb_grow(c, c->L, sizeof(H) * T * nn));
     NB_TRY(nb_grow(c, c->src, sizeof(S4) * n));
-    NB_TRY(nb_grow(c, c->pend_off, sizeof(uint32_t) * nn));
-    NB_TRY(nb_grow(c, c->pend_cnt, sizeof(uint32_t) * nn));
-    NB_TRY(nb_grow(c, c->p2p_off, sizeof(uint32_t) * nn));
-    NB_TRY(nb_grow(c, c->p2p_cnt, sizeof(uint32_t) * nn));
     float* M32 = MODE == NBODY_PREC_MIXED ? DP<float>(c->M32) : nullptr;
     const BoxDev* box = DP<BoxDev>(c->box);
 
@@ -1000,85 +748,7 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     }
     if (c->timing) cudaEventRecord(c->ev[4], c->st);
 
-    NB_TRY(nb_grow(c, c->m2l_off, sizeof(uint32_t) * nn));
-    NB_TRY(nb_grow(c, c->m2l_cnt, sizeof(uint32_t) * nn));
-    for (int attempt = 0; attempt < 8; ++attempt) {
-        size_t want_pend = (size_t)64 * nn + 1024, want_p2p = (size_t)96 * c->nleaves + 1024;
-        size_t want_m2l = (size_t)512 * nn + 1024;
-        if (c->pend_cap < want_pend) c->pend_cap = want_pend;
-        if (c->p2p_cap < want_p2p) c->p2p_cap = want_p2p;
-        if (c->m2l_cap < want_m2l) c->m2l_cap = want_m2l;
-        c->pend_cap = std::min<size_t>(c->pend_cap, 0xffffffffu);
-        c->p2p_cap = std::min<size_t>(c->p2p_cap, 0xffffffffu);
-        c->m2l_cap = std::min<size_t>(c->m2l_cap, 0xffffffffu);
-        NB_TRY(nb_grow(c, c->pend_list, sizeof(uint32_t) * c->pend_cap));
-        NB_TRY(nb_grow(c, c->p2p_list, sizeof(uint32_t) * c->p2p_cap));
-        NB_TRY(nb_grow(c, c->m2l_list, sizeof(uint32_t) * c->m2l_cap));
-        int32_t* info = DP<int32_t>(c->info);
-        NB_TRY(nb_grow(c, c->stats, 8 * sizeof(unsigned long long)));
-        NB_CU(c, cudaMemsetAsync(c->stats.p, 0, 8 * sizeof(unsigned long long), c->st));
-        NB_CU(c, cudaMemsetAsync(info + INFO_PEND_TAIL, 0, 3 * sizeof(int32_t), c->st));
-        NB_CU(c, cudaMemsetAsync(info + INFO_ERR, 0, sizeof(int32_t), c->st));
-        k_root<MODE, P><<<1, 32, 0, c->st>>>(DP<NodeRec>(c->nodes), DP<uint32_t>(c->pend_off),
-                                             DP<uint32_t>(c->pend_cnt), DP<uint32_t>(c->pend_list),
-                                             DP<uint32_t>(c->p2p_off), DP<uint32_t>(c->p2p_cnt),
-                                             DP<uint32_t>(c->p2p_list), DP<uint32_t>(c->m2l_off),
-                                             DP<uint32_t>(c->m2l_cnt), info);
-        NB_LAUNCHED(c, "root");
-        c->launches += 1;
-        ClassArgs A;
-        A.nodes = DP<NodeRec>(c->nodes);
-        A.pend_off = DP<uint32_t>(c->pend_off); A.pend_cnt = DP<uint32_t>(c->pend_cnt);
-        A.pend_list = DP<uint32_t>(c->pend_list);
-        A.p2p_off = DP<uint32_t>(c->p2p_off); A.p2p_cnt = DP<uint32_t>(c->p2p_cnt);
-        A.p2p_list = DP<uint32_t>(c->p2p_list);
-        A.m2l_off = DP<uint32_t>(c->m2l_off); A.m2l_cnt = DP<uint32_t>(c->m2l_cnt);
-        A.m2l_list = DP<uint32_t>(c->m2l_list);
-        A.pend_cap = (uint32_t)c->pend_cap; A.p2p_cap = (uint32_t)c->p2p_cap; A.m2l_cap = (uint32_t)c->m2l_cap;
-        A.stats = DP<unsigned long long>(c->stats);
-        A.info = info;
-        const float th = (float)c->prm.theta;
-        A.theta2 = th * th;
-        for (int r = 1; r <= c->depth; ++r) {
-            A.lo = c->level_start[r];
-            A.hi = c->level_start[r + 1];
-            if (A.hi <= A.lo) continue;
-            k_classify<<<(unsigned)((A.hi - A.lo + CLS_WARPS - 1) / CLS_WARPS), 32 * CLS_WARPS, 0, c->st>>>(A);
-            NB_LAUNCHED(c, "classify");
-            c->launches += 1;
-        }
-        // near-field work plan: chunks per leaf and partial-sum slots, scanned
-        {
-            const int64_t nl = c->nleaves;
-            NB_TRY(nb_grow(c, c->p2p_nch, sizeof(uint32_t) * (nl + 1)));
-            NB_TRY(nb_grow(c, c->p2p_work_off, sizeof(uint32_t) * (nl + 1)));
-            NB_TRY(nb_grow(c, c->p2p_psize, sizeof(uint32_t) * (nl + 1)));
-            NB_TRY(nb_grow(c, c->p2p_part_off, sizeof(uint32_t) * (nl + 1)));
-            k_p2p_plan<<<(unsigned)((nl + 1 + 255) / 256), 256, 0, c->st>>>(
-                nl, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes), DP<uint32_t>(c->p2p_cnt), DP<uint32_t>(c->p2p_nch),
-                DP<uint32_t>(c->p2p_psize));
-            NB_LAUNCHED(c, "p2p_plan");
-            c->launches += 1;
-            NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->p2p_nch), DP<uint32_t>(c->p2p_work_off), nl + 1,
-                               (uint32_t*)(info + INFO_P2P_WORK)));
-            NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->p2p_psize), DP<uint32_t>(c->p2p_part_off), nl + 1,
-                               (uint32_t*)(info + INFO_P2P_PART)));
-        }
-        NB_CU(c, cudaMemcpyAsync(c->h_info, info, sizeof(int32_t) * INFO_WORDS, cudaMemcpyDeviceToHost, c->st));
-        NB_CU(c, cudaMemcpyAsync(c->h_stats, c->stats.p, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                                 c->st));
-        NB_CU(c, cudaStreamSynchronize(c->st));
-        const uint32_t e = (uint32_t)c->h_info[INFO_ERR];
-        if (e & NB_ERRBIT_STACK) return nb_fail(c, NBODY_ERR_CAPACITY, "traversal descent stack overflow");
-        if (!(e & (NB_ERRBIT_PEND_CAP | NB_ERRBIT_P2P_CAP | NB_ERRBIT_M2L_CAP))) break;
-        if (e & NB_ERRBIT_M2L_CAP)
-            c->m2l_cap = std::max<size_t>(2 * c->m2l_cap, (size_t)(uint32_t)c->h_info[INFO_M2L_TAIL] + 1024);
-        if (e & NB_ERRBIT_PEND_CAP)
-            c->pend_cap = std::max<size_t>(2 * c->pend_cap, (size_t)(uint32_t)c->h_info[INFO_PEND_TAIL] + 1024);
-        if (e & NB_ERRBIT_P2P_CAP)
-            c->p2p_cap = std::max<size_t>(2 * c->p2p_cap, (size_t)(uint32_t)c->h_info[INFO_P2P_TAIL] + 1024);
-        if (attempt == 7) return nb_fail(c, NBODY_ERR_CAPACITY, "interaction lists kept overflowing");
-    }
+    NB_TRY(nb_build_lists(c));
     if (c->timing) cudaEventRecord(c->ev[5], c->st);
     {
         M2LArgs B;

@@ -1,0 +1,421 @@
+// Interaction lists of the step: far-field (M2L) and near-field (P2P) lists
+// of every cell, built breadth first.  Replaces the interaction finding of
+// src/interaction.cl:10-100 (same acceptance test and split rules,
+// reorganised per target; the resulting pair sets are the reference's).
+//
+// Level r = 1 .. depth processes the active targets of the level: every node
+// at level r, with the pending partners of its parent as input, and every
+// leaf above level r that still has pending partners of its own.  A
+// candidate is a child of an input partner, or the partner itself if it is a
+// leaf.  The candidate s of target t goes to
+//   the far-field list      if the MAC holds (and s != t),
+//   the near-field list     if t and s are leaves,
+//   t's pending list        otherwise (t internal: refined by t's children at
+//                           level r+1; t a leaf: refined by t itself at r+1).
+// Work is split into items (target, chunk of 32 input partners) so a target
+// with a long input list (a large sparse leaf next to a dense region) is
+// spread over many warps.  Each level runs a count pass and a write pass with
+// exclusive scans in between, so every target's output of the level is one
+// contiguous block in a fixed order; a final pass concatenates each target's
+// blocks in level order into the per-target lists the far- and near-field
+// kernels read.  Nothing depends on scheduling: the lists are bitwise
+// reproducible.
+#include <algorithm>
+
+#include "nbody_internal.cuh"
+
+namespace {
+
+constexpr uint32_t NONE = 0xffffffffu;
+constexpr int LW = 8;                 // warps per block of the item kernels
+constexpr int CANDS = 256;            // candidates of one item (32 partners x 8 children)
+
+struct LevelArgs {
+    const NodeRec* nodes;
+    int r, hi, nn;
+    float theta2;
+    const uint32_t *pin_off, *pin_cnt, *pin_list;     // pending input (level r - 1)
+    uint32_t *pout_off, *pout_cnt, *pout_list;        // pending output (level r)
+    uint32_t pend_cap;
+    uint32_t *nch, *first, *target;                   // items: chunks per target, first item, item -> target
+    uint32_t item_cap;
+    uint32_t* cnt[3];                                 // per item: far, near, pending outputs
+    uint32_t* off[3];                                 // their exclusive scans
+    uint32_t *m2l_stage, *p2p_stage;
+    uint32_t m2l_cap, p2p_cap;
+    uint32_t *m2l_soff, *m2l_scnt, *p2p_soff, *p2p_scnt;   // rows of level r
+    int32_t* info;
+    unsigned long long* stats;
+};
+
+__device__ __forceinline__ bool active_target(const NodeRec& nd, int r) {
+    return nd.level == r || (nd.nchild == 0 && nd.level < r);
+}
+
+// pending input of an active target: its parent's (a node of this level) or its own (a carried leaf)
+__device__ __forceinline__ void target_input(const LevelArgs& A, uint32_t t, const NodeRec& nd, uint32_t& off,
+                                             uint32_t& cnt) {
+    const uint32_t src = nd.level == A.r ? (uint32_t)nd.parent : t;
+    off = A.pin_off[src];
+    cnt = A.pin_cnt[src];
+}
+
+constexpr uint32_t LIST_CAP_BITS = NB_ERRBIT_PEND_CAP | NB_ERRBIT_P2P_CAP | NB_ERRBIT_M2L_CAP | NB_ERRBIT_ITEM_CAP;
+
+// after a capacity overflow the offsets of the failed level can point past the buffers: later
+// levels and the concatenation then do nothing (the host retries with larger capacities)
+__device__ __forceinline__ bool lists_failed(const int32_t* info) {
+    return ((uint32_t)*(volatile const int32_t*)&info[INFO_ERR] & LIST_CAP_BITS) != 0;
+}
+
+__global__ void k_lv_plan(LevelArgs A) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool failed = lists_failed(A.info);
+    if (t == 0) {
+        // running bases of the staged lists: add the previous level's totals
+        A.info[INFO_BASE_M2L] += A.info[INFO_LVL_M2L];
+        A.info[INFO_BASE_P2P] += A.info[INFO_LVL_P2P];
+    }
+    if (t > A.hi) return;
+    if (t == A.hi) { A.nch[t] = 0; return; }
+    const NodeRec nd = A.nodes[t];
+    uint32_t n = 0;
+    if (!failed && active_target(nd, A.r)) {
+        uint32_t off, cnt;
+        target_input(A, t, nd, off, cnt);
+        n = (cnt + 31) / 32;
+    }
+    A.nch[t] = n;
+    A.pout_cnt[t] = 0;
+    A.m2l_scnt[t] = 0;
+    A.p2p_scnt[t] = 0;
+}
+
+__global__ void k_lv_fill(LevelArgs A) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.hi) return;
+    const uint32_t n = A.nch[t], f = A.first[t];
+    if (n == 0) return;
+    if ((uint64_t)f + n > A.item_cap) {
+        atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_ITEM_CAP);
+        return;
+    }
+    for (uint32_t c = 0; c < n; ++c) A.target[f + c] = (uint32_t)t;
+}
+
+// Classifies the candidates of item i; WRITE = false counts, true writes.
+template <bool WRITE>
+__device__ void lv_item(const LevelArgs& A, uint32_t i, uint32_t* cand) {
+    const int lane = lane_id();
+    const uint32_t t = A.target[i];
+    const NodeRec nt = A.nodes[t];
+    const bool tleaf = nt.nchild == 0;
+    int tcx, tcy, tcz;
+    centre_fine32(nt, tcx, tcy, tcz);
+    const float tw = (float)(1u << (NB_LEVELS + 1 - nt.level));
+    uint32_t poff, pcnt;
+    target_input(A, t, nt, poff, pcnt);
+    const uint32_t chunk = i - A.first[t];
+    const uint32_t j = chunk * 32 + lane;
+    uint32_t s = NONE, ns = 0, cb = 0;
+    if (j < pcnt) {
+        s = A.pin_list[poff + j];
+        const NodeRec sn = A.nodes[s];
+        ns = sn.nchild ? sn.nchild : 1u;
+        cb = sn.nchild ? (uint32_t)sn.child_begin : s;
+    }
+    const uint32_t inc = warp_incl_scan(ns);
+    const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+    for (uint32_t u = 0; u < ns; ++u) cand[inc - ns + u] = cb + u;
+    __syncwarp();
+    // output positions of this item (write pass)
+    uint32_t o_m = 0, o_p = 0, o_q = 0;
+    bool ok_m = true, ok_p = true, ok_q = true;
+    if (WRITE) {
+        const uint32_t bm = (uint32_t)A.info[INFO_BASE_M2L], bp = (uint32_t)A.info[INFO_BASE_P2P];
+        o_m = bm + A.off[0][i];
+        o_p = bp + A.off[1][i];
+        o_q = A.off[2][i];
+        ok_m = (uint64_t)o_m + A.cnt[0][i] <= A.m2l_cap;
+        ok_p = (uint64_t)o_p + A.cnt[1][i] <= A.p2p_cap;
+        ok_q = (uint64_t)o_q + A.cnt[2][i] <= A.pend_cap;
+        if (lane == 0 && !(ok_m && ok_p && ok_q))
+            atomicOr((unsigned int*)&A.info[INFO_ERR],
+                     (ok_m ? 0u : NB_ERRBIT_M2L_CAP) | (ok_p ? 0u : NB_ERRBIT_P2P_CAP) | (ok_q ? 0u : NB_ERRBIT_PEND_CAP));
+    }
+    uint32_t nm = 0, np = 0, nq = 0;
+    unsigned long long near_particles = 0;
+    for (uint32_t g = 0; g < total; g += 32) {
+        const uint32_t sc = g + lane < total ? cand[g + lane] : NONE;
+        const bool valid = sc != NONE;
+        NodeRec sn;
+        sn.nchild = 0;
+        sn.count = 0;
+        if (valid) sn = A.nodes[sc];
+        const bool approx = valid && sc != t && mac_f32(tcx, tcy, tcz, tw, sn, A.theta2);
+        const bool sleaf = valid && sn.nchild == 0;
+        const bool near = valid && !approx && tleaf && sleaf;
+        const bool pend = valid && !approx && !near;
+        const uint32_t mm = __ballot_sync(0xffffffffu, approx);
+        const uint32_t mp = __ballot_sync(0xffffffffu, near);
+        const uint32_t mq = __ballot_sync(0xffffffffu, pend);
+        if (WRITE) {
+            const uint32_t lt = lanemask_lt();
+            if (approx && ok_m) A.m2l_stage[o_m + nm + __popc(mm & lt)] = sc;
+            if (near && ok_p) A.p2p_stage[o_p + np + __popc(mp & lt)] = sc;
+            if (pend && ok_q) A.pout_list[o_q + nq + __popc(mq & lt)] = sc;
+            if (near) near_particles += sn.count;
+        }
+        nm += __popc(mm);
+        np += __popc(mp);
+        nq += __popc(mq);
+    }
+    if (!WRITE) {
+        if (lane == 0) { A.cnt[0][i] = nm; A.cnt[1][i] = np; A.cnt[2][i] = nq; }
+        return;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) near_particles += __shfl_xor_sync(0xffffffffu, near_particles, o);
+    if (lane == 0) {
+        if (near_particles) atomicAdd(&A.stats[1], near_particles * nt.count);
+        if (chunk == 0) {
+            // the target's blocks of this level: its first item's offset, through the end of its last
+            const uint32_t e = i + A.nch[t];
+            A.m2l_soff[t] = o_m;
+            A.m2l_scnt[t] = A.off[0][e] - A.off[0][i];
+            A.p2p_soff[t] = o_p;
+            A.p2p_scnt[t] = A.off[1][e] - A.off[1][i];
+            A.pout_off[t] = o_q;
+            A.pout_cnt[t] = A.off[2][e] - A.off[2][i];
+        }
+    }
+}
+
+template <bool WRITE>
+__global__ void __launch_bounds__(32 * LW) k_lv_items(LevelArgs A) {
+    __shared__ uint32_t s_cand[LW][CANDS];
+    const uint32_t items = (uint32_t)A.info[INFO_ITEMS];
+    if (items > A.item_cap || lists_failed(A.info)) return;
+    const uint32_t stride = gridDim.x * LW;
+    for (uint32_t i = blockIdx.x * LW + (threadIdx.x >> 5); i < items; i += stride) {
+        lv_item<WRITE>(A, i, s_cand[threadIdx.x >> 5]);
+        __syncwarp();
+    }
+}
+
+struct CompactArgs {
+    const NodeRec* nodes;
+    int nn, depth;
+    const uint32_t *m2l_soff, *m2l_scnt, *p2p_soff, *p2p_scnt;   // (depth + 1) rows of nn
+    uint32_t *m2l_cnt, *p2p_cnt, *m2l_off, *p2p_off;
+    const uint32_t *m2l_stage, *p2p_stage;
+    uint32_t *m2l_list, *p2p_list;
+};
+
+// rows read for node t: its own level through the deepest (only leaves have more than one)
+__global__ void k_lv_totals(CompactArgs A) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.nn) return;
+    const NodeRec nd = A.nodes[t];
+    const int last = nd.nchild ? nd.level : A.depth;
+    uint32_t m = 0, p = 0;
+    for (int l = nd.level; l <= last; ++l) {
+        m += A.m2l_scnt[(size_t)l * A.nn + t];
+        p += A.p2p_scnt[(size_t)l * A.nn + t];
+    }
+    A.m2l_cnt[t] = m;
+    A.p2p_cnt[t] = p;
+}
+
+__global__ void __launch_bounds__(256) k_lv_concat(CompactArgs A, const int32_t* info) {
+    const int t = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = lane_id();
+    if (t >= A.nn || lists_failed(info)) return;
+    const NodeRec nd = A.nodes[t];
+    const int last = nd.nchild ? nd.level : A.depth;
+    uint32_t om = A.m2l_off[t], op = A.p2p_off[t];
+    for (int l = nd.level; l <= last; ++l) {
+        const size_t row = (size_t)l * A.nn + t;
+        const uint32_t sm = A.m2l_soff[row], cm = A.m2l_scnt[row];
+        for (uint32_t k = lane; k < cm; k += 32) A.m2l_list[om + k] = A.m2l_stage[sm + k];
+        om += cm;
+        const uint32_t sp = A.p2p_soff[row], cp = A.p2p_scnt[row];
+        for (uint32_t k = lane; k < cp; k += 32) A.p2p_list[op + k] = A.p2p_stage[sp + k];
+        op += cp;
+    }
+}
+
+__global__ void k_lv_root(const NodeRec* nodes, uint32_t* pend_off, uint32_t* pend_cnt, uint32_t* pend_list,
+                          uint32_t* m2l_soff, uint32_t* m2l_scnt, uint32_t* p2p_soff, uint32_t* p2p_scnt,
+                          uint32_t* p2p_stage, int32_t* info) {
+    if (threadIdx.x != 0) return;
+    const bool leaf = nodes[0].nchild == 0;
+    pend_off[0] = 0;
+    pend_cnt[0] = leaf ? 0u : 1u;
+    pend_list[0] = 0;
+    m2l_soff[0] = 0;
+    m2l_scnt[0] = 0;
+    p2p_soff[0] = 0;
+    p2p_scnt[0] = leaf ? 1u : 0u;
+    if (leaf) p2p_stage[0] = 0;
+    info[INFO_BASE_M2L] = 0;
+    info[INFO_BASE_P2P] = 0;
+    info[INFO_LVL_M2L] = 0;
+    info[INFO_LVL_P2P] = leaf ? 1 : 0;
+}
+
+// near-field work plan: chunks of P2P_LEAF_CHUNK partner leaves per leaf and partial-sum slots
+__global__ void k_p2p_plan(int64_t nleaves, const uint32_t* __restrict__ leaves, const NodeRec* __restrict__ nodes,
+                           const uint32_t* __restrict__ p2p_cnt, uint32_t* __restrict__ nch,
+                           uint32_t* __restrict__ psize) {
+    const int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li > nleaves) return;
+    if (li == nleaves) { nch[li] = 0; psize[li] = 0; return; }
+    const uint32_t k = leaves[li];
+    const uint32_t c = (p2p_cnt[k] + NB_P2P_CHUNK - 1) / NB_P2P_CHUNK;
+    const uint32_t n = c > 1 ? c : 1u;
+    nch[li] = n;
+    psize[li] = n > 1 ? n * nodes[k].count : 0u;
+}
+
+}  // namespace
+
+int nb_build_lists(nbody_ctx* c) {
+    const int64_t nn = c->nnodes, nl = c->nleaves;
+    const int depth = c->depth;
+    const size_t rows = (size_t)(depth + 1) * nn;
+    NB_TRY(nb_grow(c, c->pend_off, sizeof(uint32_t) * 2 * nn));
+    NB_TRY(nb_grow(c, c->pend_cnt, sizeof(uint32_t) * 2 * nn));
+    NB_TRY(nb_grow(c, c->m2l_off, sizeof(uint32_t) * (nn + 1)));
+    NB_TRY(nb_grow(c, c->m2l_cnt, sizeof(uint32_t) * (nn + 1)));
+    NB_TRY(nb_grow(c, c->p2p_off, sizeof(uint32_t) * (nn + 1)));
+    NB_TRY(nb_grow(c, c->p2p_cnt, sizeof(uint32_t) * (nn + 1)));
+    NB_TRY(nb_grow(c, c->lst_seg, sizeof(uint32_t) * 4 * rows));
+    NB_TRY(nb_grow(c, c->lst_nch, sizeof(uint32_t) * (nn + 1)));
+    NB_TRY(nb_grow(c, c->lst_first, sizeof(uint32_t) * (nn + 1)));
+    NB_TRY(nb_grow(c, c->stats, 8 * sizeof(unsigned long long)));
+    uint32_t* seg = DP<uint32_t>(c->lst_seg);
+    int32_t* info = DP<int32_t>(c->info);
+    const int sms = 152;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        c->pend_cap = std::min<size_t>(std::max<size_t>(c->pend_cap, (size_t)64 * nn + 1024), 0xffffffffu);
+        c->p2p_cap = std::min<size_t>(std::max<size_t>(c->p2p_cap, (size_t)96 * nl + 1024), 0xffffffffu);
+        c->m2l_cap = std::min<size_t>(std::max<size_t>(c->m2l_cap, (size_t)512 * nn + 1024), 0xffffffffu);
+        c->item_cap = std::min<size_t>(std::max<size_t>(c->item_cap, (size_t)4 * nn + 4096), 0xffffffffu);
+        NB_TRY(nb_grow(c, c->pend_list, sizeof(uint32_t) * 2 * c->pend_cap));
+        NB_TRY(nb_grow(c, c->p2p_list, sizeof(uint32_t) * c->p2p_cap));
+        NB_TRY(nb_grow(c, c->m2l_list, sizeof(uint32_t) * c->m2l_cap));
+        NB_TRY(nb_grow(c, c->p2p_stage, sizeof(uint32_t) * c->p2p_cap));
+        NB_TRY(nb_grow(c, c->m2l_stage, sizeof(uint32_t) * c->m2l_cap));
+        NB_TRY(nb_grow(c, c->lst_target, sizeof(uint32_t) * c->item_cap));
+        NB_TRY(nb_grow(c, c->lst_cnt, sizeof(uint32_t) * 3 * (c->item_cap + 1)));
+        NB_TRY(nb_grow(c, c->lst_off, sizeof(uint32_t) * 3 * (c->item_cap + 1)));
+        NB_CU(c, cudaMemsetAsync(c->stats.p, 0, 8 * sizeof(unsigned long long), c->st));
+        NB_CU(c, cudaMemsetAsync(info + INFO_ERR, 0, sizeof(int32_t), c->st));
+        uint32_t* pend_off = DP<uint32_t>(c->pend_off);
+        uint32_t* pend_cnt = DP<uint32_t>(c->pend_cnt);
+        uint32_t* pend_list = DP<uint32_t>(c->pend_list);
+        uint32_t* cnt = DP<uint32_t>(c->lst_cnt);
+        uint32_t* off = DP<uint32_t>(c->lst_off);
+        const size_t ic = c->item_cap + 1;
+        k_lv_root<<<1, 32, 0, c->st>>>(DP<NodeRec>(c->nodes), pend_off, pend_cnt, pend_list, seg + 0 * rows,
+                                       seg + 1 * rows, seg + 2 * rows, seg + 3 * rows, DP<uint32_t>(c->p2p_stage),
+                                       info);
+        NB_LAUNCHED(c, "lists root");
+        c->launches += 1;
+        LevelArgs A;
+        A.nodes = DP<NodeRec>(c->nodes);
+        A.nn = (int)nn;
+        const float th = (float)c->prm.theta;
+        A.theta2 = th * th;
+        A.pend_cap = (uint32_t)c->pend_cap;
+        A.nch = DP<uint32_t>(c->lst_nch);
+        A.first = DP<uint32_t>(c->lst_first);
+        A.target = DP<uint32_t>(c->lst_target);
+        A.item_cap = (uint32_t)c->item_cap;
+        for (int k = 0; k < 3; ++k) { A.cnt[k] = cnt + k * ic; A.off[k] = off + k * ic; }
+        A.m2l_stage = DP<uint32_t>(c->m2l_stage);
+        A.p2p_stage = DP<uint32_t>(c->p2p_stage);
+        A.m2l_cap = (uint32_t)c->m2l_cap;
+        A.p2p_cap = (uint32_t)c->p2p_cap;
+        A.info = info;
+        A.stats = DP<unsigned long long>(c->stats);
+        for (int r = 1; r <= depth; ++r) {
+            const int pi = (r - 1) & 1, po = r & 1;
+            A.r = r;
+            A.hi = c->level_start[r + 1];
+            A.pin_off = pend_off + pi * nn; A.pin_cnt = pend_cnt + pi * nn; A.pin_list = pend_list + pi * c->pend_cap;
+            A.pout_off = pend_off + po * nn; A.pout_cnt = pend_cnt + po * nn; A.pout_list = pend_list + po * c->pend_cap;
+            A.m2l_soff = seg + 0 * rows + (size_t)r * nn;
+            A.m2l_scnt = seg + 1 * rows + (size_t)r * nn;
+            A.p2p_soff = seg + 2 * rows + (size_t)r * nn;
+            A.p2p_scnt = seg + 3 * rows + (size_t)r * nn;
+            const unsigned gt = (unsigned)((A.hi + 1 + 255) / 256);
+            k_lv_plan<<<gt, 256, 0, c->st>>>(A);
+            NB_LAUNCHED(c, "lists plan");
+            NB_TRY(nb_scan_u32(c, A.nch, A.first, A.hi + 1, (uint32_t*)(info + INFO_ITEMS)));
+            k_lv_fill<<<gt, 256, 0, c->st>>>(A);
+            NB_CU(c, cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * 3 * ic, c->st));
+            k_lv_items<false><<<sms * 8, 32 * LW, 0, c->st>>>(A);
+            NB_LAUNCHED(c, "lists count");
+            // per-item offsets; one extra entry past the last item gives each target's end
+            {
+                const uint32_t* in3[3] = {A.cnt[0], A.cnt[1], A.cnt[2]};
+                uint32_t* out3[3] = {A.off[0], A.off[1], A.off[2]};
+                uint32_t* tot3[3] = {(uint32_t*)(info + INFO_LVL_M2L), (uint32_t*)(info + INFO_LVL_P2P),
+                                     (uint32_t*)(info + INFO_LVL_PEND)};
+                NB_TRY(nb_scan3_u32(c, in3, out3, (int64_t)c->item_cap + 1, tot3));
+            }
+            k_lv_items<true><<<sms * 8, 32 * LW, 0, c->st>>>(A);
+            NB_LAUNCHED(c, "lists write");
+            c->launches += 4;
+        }
+        // concatenate each target's blocks in level order
+        CompactArgs B;
+        B.nodes = DP<NodeRec>(c->nodes);
+        B.nn = (int)nn;
+        B.depth = depth;
+        B.m2l_soff = seg; B.m2l_scnt = seg + rows; B.p2p_soff = seg + 2 * rows; B.p2p_scnt = seg + 3 * rows;
+        B.m2l_cnt = DP<uint32_t>(c->m2l_cnt); B.p2p_cnt = DP<uint32_t>(c->p2p_cnt);
+        B.m2l_off = DP<uint32_t>(c->m2l_off); B.p2p_off = DP<uint32_t>(c->p2p_off);
+        B.m2l_stage = DP<uint32_t>(c->m2l_stage); B.p2p_stage = DP<uint32_t>(c->p2p_stage);
+        B.m2l_list = DP<uint32_t>(c->m2l_list); B.p2p_list = DP<uint32_t>(c->p2p_list);
+        k_lv_totals<<<(unsigned)((nn + 255) / 256), 256, 0, c->st>>>(B);
+        NB_LAUNCHED(c, "lists totals");
+        NB_TRY(nb_scan_u32(c, B.m2l_cnt, B.m2l_off, nn, (uint32_t*)(info + INFO_M2L_TAIL)));
+        NB_TRY(nb_scan_u32(c, B.p2p_cnt, B.p2p_off, nn, (uint32_t*)(info + INFO_P2P_TAIL)));
+        k_lv_concat<<<(unsigned)((nn + 7) / 8), 256, 0, c->st>>>(B, info);
+        NB_LAUNCHED(c, "lists concat");
+        c->launches += 2;
+        // near-field work plan
+        NB_TRY(nb_grow(c, c->p2p_nch, sizeof(uint32_t) * (nl + 1)));
+        NB_TRY(nb_grow(c, c->p2p_work_off, sizeof(uint32_t) * (nl + 1)));
+        NB_TRY(nb_grow(c, c->p2p_psize, sizeof(uint32_t) * (nl + 1)));
+        NB_TRY(nb_grow(c, c->p2p_part_off, sizeof(uint32_t) * (nl + 1)));
+        k_p2p_plan<<<(unsigned)((nl + 1 + 255) / 256), 256, 0, c->st>>>(nl, DP<uint32_t>(c->leaves),
+                                                                         DP<NodeRec>(c->nodes), B.p2p_cnt,
+                                                                         DP<uint32_t>(c->p2p_nch),
+                                                                         DP<uint32_t>(c->p2p_psize));
+        NB_LAUNCHED(c, "p2p plan");
+        c->launches += 1;
+        NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->p2p_nch), DP<uint32_t>(c->p2p_work_off), nl + 1,
+                           (uint32_t*)(info + INFO_P2P_WORK)));
+        NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->p2p_psize), DP<uint32_t>(c->p2p_part_off), nl + 1,
+                           (uint32_t*)(info + INFO_P2P_PART)));
+        NB_CU(c, cudaMemcpyAsync(c->h_info, info, sizeof(int32_t) * INFO_WORDS, cudaMemcpyDeviceToHost, c->st));
+        NB_CU(c, cudaMemcpyAsync(c->h_stats, c->stats.p, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 c->st));
+        NB_CU(c, cudaStreamSynchronize(c->st));
+        c->h_stats[0] = (uint32_t)c->h_info[INFO_M2L_TAIL];
+        c->h_stats[2] = (uint32_t)c->h_info[INFO_P2P_TAIL];
+        const uint32_t e = (uint32_t)c->h_info[INFO_ERR];
+        const uint32_t caps = NB_ERRBIT_PEND_CAP | NB_ERRBIT_P2P_CAP | NB_ERRBIT_M2L_CAP | NB_ERRBIT_ITEM_CAP;
+        if (!(e & caps)) return NBODY_OK;
+        if (attempt == 7) break;
+        if (e & NB_ERRBIT_M2L_CAP) c->m2l_cap *= 2;
+        if (e & NB_ERRBIT_PEND_CAP) c->pend_cap *= 2;
+        if (e & NB_ERRBIT_P2P_CAP) c->p2p_cap *= 2;
+        if (e & NB_ERRBIT_ITEM_CAP) c->item_cap *= 2;
+    }
+    return nb_fail(c, NBODY_ERR_CAPACITY, "interaction lists kept overflowing");
+}

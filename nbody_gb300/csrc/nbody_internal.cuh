@@ -16,11 +16,13 @@
 // error bits raised on the device (ctx->d_info[INFO_ERR])
 #define NB_ERRBIT_PEND_CAP 1u      // refinement list capacity exceeded
 #define NB_ERRBIT_P2P_CAP 2u       // near-field list capacity exceeded
-#define NB_ERRBIT_STACK 4u         // per-warp descent stack overflow
 #define NB_ERRBIT_RANGE 8u         // a particle lay outside a fixed root box
 #define NB_ERRBIT_NONFINITE 16u    // a position was not finite
 #define NB_ERRBIT_M2L_CAP 32u      // far-field list capacity exceeded
 #define NB_ERRBIT_ASYNC 64u        // an asynchronous copy did not complete within its time limit
+#define NB_ERRBIT_ITEM_CAP 128u    // list-building work items exceeded their capacity
+
+#define NB_P2P_CHUNK 256           // partner leaves per near-field work item
 
 // layout of the small device info block (int32 words)
 enum {
@@ -34,7 +36,13 @@ enum {
     INFO_HIST = 8,                 // 8 .. 8+NB_LEVELS: nodes per level
     INFO_P2P_WORK = 30,            // near-field work items
     INFO_P2P_PART = 31,            // near-field partial-sum slots
-    INFO_WORDS = 32
+    INFO_ITEMS = 32,               // list-building items of the current level
+    INFO_LVL_M2L = 33,             // far-field entries written by the current level
+    INFO_LVL_P2P = 34,             // near-field entries written by the current level
+    INFO_LVL_PEND = 35,            // pending entries written by the current level
+    INFO_BASE_M2L = 36,            // staged far-field entries of the levels before
+    INFO_BASE_P2P = 37,            // staged near-field entries of the levels before
+    INFO_WORDS = 40
 };
 
 // one octree node, breadth-first order, 32 bytes
@@ -85,10 +93,11 @@ struct nbody_ctx {
 
     // expansions and lists
     DevBuf M, M32, L, src;
-    DevBuf pend_off, pend_cnt, p2p_off, p2p_cnt, pend_list, p2p_list;
-    size_t pend_cap = 0, p2p_cap = 0;
-    DevBuf m2l_off, m2l_cnt, m2l_list;
-    size_t m2l_cap = 0;
+    DevBuf pend_off, pend_cnt, pend_list;          // pending lists, two level parities
+    DevBuf p2p_off, p2p_cnt, p2p_list, m2l_off, m2l_cnt, m2l_list;   // per-target lists
+    DevBuf p2p_stage, m2l_stage;                    // per-level blocks before concatenation
+    DevBuf lst_seg, lst_nch, lst_first, lst_target, lst_cnt, lst_off;   // list-building work
+    size_t pend_cap = 0, p2p_cap = 0, m2l_cap = 0, item_cap = 0;
     DevBuf stage;                  // host <-> device staging (interleaved doubles)
     DevBuf diag;
     DevBuf stats;                  // 8 x uint64 work counters of the last evaluation
@@ -138,6 +147,8 @@ static inline T* DP(const DevBuf& b) { return reinterpret_cast<T*>(b.p); }
 
 // scan + sort (sort.cu)
 int nb_scan_u32(nbody_ctx* c, const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total_dev);
+int nb_scan3_u32(nbody_ctx* c, const uint32_t* const in[3], uint32_t* const out[3], int64_t n,
+                 uint32_t* const total_dev[3]);
 int nb_radix_sort(nbody_ctx* c, int64_t n, uint64_t* k0, uint32_t* v0, uint64_t* k1, uint32_t* v1, int begin_bit,
                   int end_bit, int* result_in_first);
 
@@ -145,6 +156,9 @@ int nb_radix_sort(nbody_ctx* c, int64_t n, uint64_t* k0, uint32_t* v0, uint64_t*
 int nb_begin_step(nbody_ctx* c, int kdk);
 int nb_sort_and_gather(nbody_ctx* c);
 int nb_build_tree(nbody_ctx* c);
+
+// interaction lists and near-field work plan of the current tree (lists.cu); syncs once
+int nb_build_lists(nbody_ctx* c);
 
 // one force evaluation at the current positions (api.cu); kdk = 1 applies the opening kick and drift first
 int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot);
@@ -235,3 +249,30 @@ __device__ __forceinline__ void nb_centre_fine(const NodeRec& nd, long long& cx,
     cz = (2ll * nd.iz + 1) << sh;
 }
 __device__ __forceinline__ long long nb_width_fine(const NodeRec& nd) { return 1ll << (NB_LEVELS + 1 - nd.level); }
+
+// centre (2i+1) << (21 - level) in fine units (side / 2^22); fits in 32 bits
+__device__ __forceinline__ void centre_fine32(const NodeRec& nd, int& cx, int& cy, int& cz) {
+    const int sh = NB_LEVELS - nd.level;
+    cx = (int)((2u * nd.ix + 1u) << sh);
+    cy = (int)((2u * nd.iy + 1u) << sh);
+    cz = (int)((2u * nd.iz + 1u) << sh);
+}
+
+// MAC of src/interaction.cl:64-79 in its own FP32 operation order: displacement of centres,
+// distance^2 = ((x*x + y*y) + z*z) + w*w with w = 0, extent^2 = (0.75 * (wA+wB)) * (wA+wB),
+// approximate iff extent^2 / distance^2 < theta^2 (correctly rounded division).  Lengths are in
+// fine units, an exact power-of-two rescaling of the reference's box units, so every rounding is
+// the reference's.  The division is only evaluated when a cheap estimate is within 0.1 % of the
+// threshold, where it could matter; elsewhere the estimate decides the same way.
+__device__ __forceinline__ bool mac_f32(int tcx, int tcy, int tcz, float tw, const NodeRec& s, float theta2) {
+    int sx, sy, sz;
+    centre_fine32(s, sx, sy, sz);
+    const float dx = (float)(sx - tcx), dy = (float)(sy - tcy), dz = (float)(sz - tcz);
+    const float d2 = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)), 0.0f);
+    const float es = __fadd_rn(tw, (float)(1u << (NB_LEVELS + 1 - s.level)));
+    const float e2 = __fmul_rn(__fmul_rn(0.75f, es), es);
+    const float est = __fdividef(e2, d2);   // within a few ulp of the quotient
+    if (est < 0.999f * theta2) return true;
+    if (est > 1.001f * theta2) return false;
+    return __fdiv_rn(e2, d2) < theta2;
+}

@@ -78,6 +78,68 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const uint32_t* __re
     }
 }
 
+// the same three phases over K arrays at once (one launch per phase for all of them)
+struct ScanK {
+    const uint32_t* in[3];
+    uint32_t* out[3];
+    uint32_t* total[3];
+};
+
+template <int K>
+__global__ void __launch_bounds__(SCAN_THREADS) k_scank_reduce(ScanK A, int64_t n, uint32_t* __restrict__ part,
+                                                                 int64_t nb) {
+    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        uint32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k)
+            if (base + k < n) s += A.in[a][base + k];
+        uint32_t tot;
+        block_excl_scan(s, &tot);
+        if (threadIdx.x == 0) part[a * nb + blockIdx.x] = tot;
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(1024) k_scank_partials(ScanK A, uint32_t* part, int64_t nb) {
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        uint32_t run = 0;
+        for (int64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+            const int64_t i = b0 + threadIdx.x;
+            const uint32_t v = i < nb ? part[a * nb + i] : 0u;
+            uint32_t tot;
+            const uint32_t e = block_excl_scan(v, &tot);
+            if (i < nb) part[a * nb + i] = run + e;
+            run += tot;
+        }
+        if (threadIdx.x == 0 && A.total[a]) *A.total[a] = run;
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(SCAN_THREADS) k_scank_down(ScanK A, int64_t n, const uint32_t* __restrict__ part,
+                                                               int64_t nb) {
+    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        uint32_t v[SCAN_ITEMS];
+        uint32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            v[k] = base + k < n ? A.in[a][base + k] : 0u;
+            s += v[k];
+        }
+        uint32_t e = block_excl_scan(s, nullptr) + part[a * nb + blockIdx.x];
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            if (base + k < n) A.out[a][base + k] = e;
+            e += v[k];
+        }
+    }
+}
+
 __global__ void __launch_bounds__(RADIX_THREADS) k_radix_hist(const uint64_t* __restrict__ keys, int64_t n, int shift,
                                                                 uint32_t mask, uint32_t* __restrict__ hist, int nblocks) {
     __shared__ uint32_t h[256];
@@ -151,6 +213,26 @@ int nb_scan_u32(nbody_ctx* c, const uint32_t* in, uint32_t* out, int64_t n, uint
     k_scan_partials<<<1, 1024, 0, c->st>>>(part, nb, total_dev);
     k_scan_down<<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(in, out, n, part);
     NB_LAUNCHED(c, "scan");
+    c->launches += 3;
+    return NBODY_OK;
+}
+
+int nb_scan3_u32(nbody_ctx* c, const uint32_t* const in[3], uint32_t* const out[3], int64_t n,
+                 uint32_t* const total_dev[3]) {
+    if (n <= 0) {
+        for (int a = 0; a < 3; ++a)
+            if (total_dev[a]) NB_CU(c, cudaMemsetAsync(total_dev[a], 0, sizeof(uint32_t), c->st));
+        return NBODY_OK;
+    }
+    const int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    NB_TRY(nb_grow(c, c->scan_part, sizeof(uint32_t) * (size_t)(3 * nb + 1)));
+    uint32_t* part = DP<uint32_t>(c->scan_part);
+    ScanK A;
+    for (int a = 0; a < 3; ++a) { A.in[a] = in[a]; A.out[a] = out[a]; A.total[a] = total_dev[a]; }
+    k_scank_reduce<3><<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(A, n, part, nb);
+    k_scank_partials<3><<<1, 1024, 0, c->st>>>(A, part, nb);
+    k_scank_down<3><<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(A, n, part, nb);
+    NB_LAUNCHED(c, "scan3");
     c->launches += 3;
     return NBODY_OK;
 }
