@@ -294,8 +294,8 @@ int nbody_destroy(nbody_ctx* c) {
                       &c->pend_cnt, &c->p2p_off, &c->p2p_cnt, &c->pend_list, &c->p2p_list, &c->m2l_off, &c->m2l_cnt,
                       &c->m2l_list, &c->stage, &c->diag, &c->info, &c->box, &c->bbox, &c->adj_lx, &c->adj_lv,
                       &c->adj_gq, &c->adj_gm, &c->adj_nu, &c->adj_lamL, &c->adj_lamL32, &c->adj_lamM, &c->adj_near,
-                      &c->snaps, &c->p2p_stage, &c->m2l_stage, &c->lst_seg, &c->lst_nch, &c->lst_first,
-                      &c->lst_target, &c->lst_cnt, &c->lst_off})
+                      &c->snaps, &c->lst_seg, &c->lst_nch, &c->lst_first, &c->lst_target, &c->lst_cnt,
+                      &c->lst_off, &c->lst_cp})
         release(*b);
     if (c->h_info) cudaFreeHost(c->h_info);
     for (int i = 0; i < 16; ++i)

@@ -195,6 +195,12 @@ template <bool WRITE>
 __global__ void __launch_bounds__(32 * LW) k_lv_items(LevelArgs A) {
     __shared__ uint32_t s_cand[LW][CANDS];
     const uint32_t items = (uint32_t)A.info[INFO_ITEMS];
+    if (!WRITE && blockIdx.x == 0 && threadIdx.x == 0) {
+        // the scans cover items + 1 entries: the last one (zero) gives every target's end
+        const uint32_t m = items < A.item_cap ? items : A.item_cap;
+        A.cnt[0][m] = 0; A.cnt[1][m] = 0; A.cnt[2][m] = 0;
+        A.info[INFO_ITEMS1] = (int32_t)(m + 1);
+    }
     if (items > A.item_cap || lists_failed(A.info)) return;
     const uint32_t stride = gridDim.x * LW;
     for (uint32_t i = blockIdx.x * LW + (threadIdx.x >> 5); i < items; i += stride) {
@@ -208,40 +214,91 @@ struct CompactArgs {
     int nn, depth;
     const uint32_t *m2l_soff, *m2l_scnt, *p2p_soff, *p2p_scnt;   // (depth + 1) rows of nn
     uint32_t *m2l_cnt, *p2p_cnt, *m2l_off, *p2p_off;
-    const uint32_t *m2l_stage, *p2p_stage;
+    uint32_t *m2l_cp, *p2p_cp, *m2l_cpo, *p2p_cpo;                // entries to move (multi-block targets), scanned
     uint32_t *m2l_list, *p2p_list;
+    uint32_t m2l_cap, p2p_cap;
+    int32_t* info;
+    unsigned long long* stats;
 };
 
-// rows read for node t: its own level through the deepest (only leaves have more than one)
-__global__ void k_lv_totals(CompactArgs A) {
+// Per target: list length over its rows (its own level through the deepest; only leaves have more
+// than one).  A target whose entries sit in one block keeps them in place; one with several blocks
+// gets them moved, in level order, behind the staged entries.
+__global__ void __launch_bounds__(256) k_lv_totals(CompactArgs A) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= A.nn) return;
-    const NodeRec nd = A.nodes[t];
-    const int last = nd.nchild ? nd.level : A.depth;
     uint32_t m = 0, p = 0;
-    for (int l = nd.level; l <= last; ++l) {
-        m += A.m2l_scnt[(size_t)l * A.nn + t];
-        p += A.p2p_scnt[(size_t)l * A.nn + t];
+    if (t < A.nn) {
+        const NodeRec nd = A.nodes[t];
+        const int last = nd.nchild ? nd.level : A.depth;
+        uint32_t mb = 0, pb = 0, mo = 0, po = 0;
+        for (int l = nd.level; l <= last; ++l) {
+            const size_t row = (size_t)l * A.nn + t;
+            const uint32_t cm = A.m2l_scnt[row], cp = A.p2p_scnt[row];
+            if (cm) { ++mb; mo = A.m2l_soff[row]; }
+            if (cp) { ++pb; po = A.p2p_soff[row]; }
+            m += cm;
+            p += cp;
+        }
+        A.m2l_cnt[t] = m;
+        A.p2p_cnt[t] = p;
+        A.m2l_off[t] = mb == 1 ? mo : 0u;
+        A.p2p_off[t] = pb == 1 ? po : 0u;
+        A.m2l_cp[t] = mb > 1 ? m : 0u;
+        A.p2p_cp[t] = pb > 1 ? p : 0u;
     }
-    A.m2l_cnt[t] = m;
-    A.p2p_cnt[t] = p;
+    if (t == A.nn) { A.m2l_cp[t] = 0; A.p2p_cp[t] = 0; }
+    unsigned long long m64 = m, p64 = p;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        m64 += __shfl_xor_sync(0xffffffffu, m64, o);
+        p64 += __shfl_xor_sync(0xffffffffu, p64, o);
+    }
+    if ((threadIdx.x & 31) == 0 && (m64 || p64)) {
+        atomicAdd(&A.stats[0], m64);
+        atomicAdd(&A.stats[2], p64);
+    }
 }
 
-__global__ void __launch_bounds__(256) k_lv_concat(CompactArgs A, const int32_t* info) {
-    const int t = blockIdx.x * 8 + (threadIdx.x >> 5);
-    const int lane = lane_id();
-    if (t >= A.nn || lists_failed(info)) return;
+// Moves the entries of multi-block targets behind the staged ones, one destination entry per
+// thread: the target by binary search over the moved-entry offsets, then its block by walking its
+// rows in level order.  Parallel over entries, so a long list (a large leaf with partners on many
+// levels) does not serialise on one warp.
+__device__ __forceinline__ void move_entry(const CompactArgs& A, uint32_t d, const uint32_t* cpo, const uint32_t* soff,
+                                           const uint32_t* scnt, uint32_t* list, uint32_t base, uint32_t* off) {
+    int lo = 0, hi = A.nn;                      // largest t with cpo[t] <= d
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (cpo[mid] <= d) lo = mid; else hi = mid;
+    }
+    const int t = lo;
+    uint32_t k = d - cpo[t];
+    if (k == 0) off[t] = base + cpo[t];
     const NodeRec nd = A.nodes[t];
-    const int last = nd.nchild ? nd.level : A.depth;
-    uint32_t om = A.m2l_off[t], op = A.p2p_off[t];
-    for (int l = nd.level; l <= last; ++l) {
+    for (int l = nd.level; l <= A.depth; ++l) {
         const size_t row = (size_t)l * A.nn + t;
-        const uint32_t sm = A.m2l_soff[row], cm = A.m2l_scnt[row];
-        for (uint32_t k = lane; k < cm; k += 32) A.m2l_list[om + k] = A.m2l_stage[sm + k];
-        om += cm;
-        const uint32_t sp = A.p2p_soff[row], cp = A.p2p_scnt[row];
-        for (uint32_t k = lane; k < cp; k += 32) A.p2p_list[op + k] = A.p2p_stage[sp + k];
-        op += cp;
+        const uint32_t cn = scnt[row];
+        if (k < cn) {
+            list[base + d] = list[soff[row] + k];
+            return;
+        }
+        k -= cn;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_lv_move(CompactArgs A) {
+    if (lists_failed(A.info)) return;
+    const uint32_t em = (uint32_t)(A.info[INFO_BASE_M2L] + A.info[INFO_LVL_M2L]);
+    const uint32_t ep = (uint32_t)(A.info[INFO_BASE_P2P] + A.info[INFO_LVL_P2P]);
+    const uint32_t tot_m = A.m2l_cpo[A.nn], tot_p = A.p2p_cpo[A.nn];
+    if ((uint64_t)em + tot_m > A.m2l_cap || (uint64_t)ep + tot_p > A.p2p_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_M2L_CAP | NB_ERRBIT_P2P_CAP);
+        return;
+    }
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < tot_m + tot_p; d += stride) {
+        if (d < tot_m) move_entry(A, d, A.m2l_cpo, A.m2l_soff, A.m2l_scnt, A.m2l_list, em, A.m2l_off);
+        else move_entry(A, d - tot_m, A.p2p_cpo, A.p2p_soff, A.p2p_scnt, A.p2p_list, ep, A.p2p_off);
     }
 }
 
@@ -305,8 +362,6 @@ int nb_build_lists(nbody_ctx* c) {
         NB_TRY(nb_grow(c, c->pend_list, sizeof(uint32_t) * 2 * c->pend_cap));
         NB_TRY(nb_grow(c, c->p2p_list, sizeof(uint32_t) * c->p2p_cap));
         NB_TRY(nb_grow(c, c->m2l_list, sizeof(uint32_t) * c->m2l_cap));
-        NB_TRY(nb_grow(c, c->p2p_stage, sizeof(uint32_t) * c->p2p_cap));
-        NB_TRY(nb_grow(c, c->m2l_stage, sizeof(uint32_t) * c->m2l_cap));
         NB_TRY(nb_grow(c, c->lst_target, sizeof(uint32_t) * c->item_cap));
         NB_TRY(nb_grow(c, c->lst_cnt, sizeof(uint32_t) * 3 * (c->item_cap + 1)));
         NB_TRY(nb_grow(c, c->lst_off, sizeof(uint32_t) * 3 * (c->item_cap + 1)));
@@ -319,7 +374,7 @@ int nb_build_lists(nbody_ctx* c) {
         uint32_t* off = DP<uint32_t>(c->lst_off);
         const size_t ic = c->item_cap + 1;
         k_lv_root<<<1, 32, 0, c->st>>>(DP<NodeRec>(c->nodes), pend_off, pend_cnt, pend_list, seg + 0 * rows,
-                                       seg + 1 * rows, seg + 2 * rows, seg + 3 * rows, DP<uint32_t>(c->p2p_stage),
+                                       seg + 1 * rows, seg + 2 * rows, seg + 3 * rows, DP<uint32_t>(c->p2p_list),
                                        info);
         NB_LAUNCHED(c, "lists root");
         c->launches += 1;
@@ -334,8 +389,8 @@ int nb_build_lists(nbody_ctx* c) {
         A.target = DP<uint32_t>(c->lst_target);
         A.item_cap = (uint32_t)c->item_cap;
         for (int k = 0; k < 3; ++k) { A.cnt[k] = cnt + k * ic; A.off[k] = off + k * ic; }
-        A.m2l_stage = DP<uint32_t>(c->m2l_stage);
-        A.p2p_stage = DP<uint32_t>(c->p2p_stage);
+        A.m2l_stage = DP<uint32_t>(c->m2l_list);
+        A.p2p_stage = DP<uint32_t>(c->p2p_list);
         A.m2l_cap = (uint32_t)c->m2l_cap;
         A.p2p_cap = (uint32_t)c->p2p_cap;
         A.info = info;
@@ -355,7 +410,6 @@ int nb_build_lists(nbody_ctx* c) {
             NB_LAUNCHED(c, "lists plan");
             NB_TRY(nb_scan_u32(c, A.nch, A.first, A.hi + 1, (uint32_t*)(info + INFO_ITEMS)));
             k_lv_fill<<<gt, 256, 0, c->st>>>(A);
-            NB_CU(c, cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * 3 * ic, c->st));
             k_lv_items<false><<<sms * 8, 32 * LW, 0, c->st>>>(A);
             NB_LAUNCHED(c, "lists count");
             // per-item offsets; one extra entry past the last item gives each target's end
@@ -364,13 +418,15 @@ int nb_build_lists(nbody_ctx* c) {
                 uint32_t* out3[3] = {A.off[0], A.off[1], A.off[2]};
                 uint32_t* tot3[3] = {(uint32_t*)(info + INFO_LVL_M2L), (uint32_t*)(info + INFO_LVL_P2P),
                                      (uint32_t*)(info + INFO_LVL_PEND)};
-                NB_TRY(nb_scan3_u32(c, in3, out3, (int64_t)c->item_cap + 1, tot3));
+                NB_TRY(nb_scan3_u32(c, in3, out3, (int64_t)c->item_cap + 1, tot3, (const uint32_t*)(info + INFO_ITEMS1)));
             }
             k_lv_items<true><<<sms * 8, 32 * LW, 0, c->st>>>(A);
             NB_LAUNCHED(c, "lists write");
             c->launches += 4;
         }
-        // concatenate each target's blocks in level order
+        // per-target lists: blocks left in place, multi-block targets concatenated in level order
+        NB_TRY(nb_grow(c, c->lst_cp, sizeof(uint32_t) * 4 * (nn + 1)));
+        uint32_t* cp = DP<uint32_t>(c->lst_cp);
         CompactArgs B;
         B.nodes = DP<NodeRec>(c->nodes);
         B.nn = (int)nn;
@@ -378,14 +434,21 @@ int nb_build_lists(nbody_ctx* c) {
         B.m2l_soff = seg; B.m2l_scnt = seg + rows; B.p2p_soff = seg + 2 * rows; B.p2p_scnt = seg + 3 * rows;
         B.m2l_cnt = DP<uint32_t>(c->m2l_cnt); B.p2p_cnt = DP<uint32_t>(c->p2p_cnt);
         B.m2l_off = DP<uint32_t>(c->m2l_off); B.p2p_off = DP<uint32_t>(c->p2p_off);
-        B.m2l_stage = DP<uint32_t>(c->m2l_stage); B.p2p_stage = DP<uint32_t>(c->p2p_stage);
+        B.m2l_cp = cp; B.p2p_cp = cp + (nn + 1); B.m2l_cpo = cp + 2 * (nn + 1); B.p2p_cpo = cp + 3 * (nn + 1);
         B.m2l_list = DP<uint32_t>(c->m2l_list); B.p2p_list = DP<uint32_t>(c->p2p_list);
-        k_lv_totals<<<(unsigned)((nn + 255) / 256), 256, 0, c->st>>>(B);
+        B.m2l_cap = (uint32_t)c->m2l_cap; B.p2p_cap = (uint32_t)c->p2p_cap;
+        B.info = info;
+        B.stats = DP<unsigned long long>(c->stats);
+        k_lv_totals<<<(unsigned)((nn + 1 + 255) / 256), 256, 0, c->st>>>(B);
         NB_LAUNCHED(c, "lists totals");
-        NB_TRY(nb_scan_u32(c, B.m2l_cnt, B.m2l_off, nn, (uint32_t*)(info + INFO_M2L_TAIL)));
-        NB_TRY(nb_scan_u32(c, B.p2p_cnt, B.p2p_off, nn, (uint32_t*)(info + INFO_P2P_TAIL)));
-        k_lv_concat<<<(unsigned)((nn + 7) / 8), 256, 0, c->st>>>(B, info);
-        NB_LAUNCHED(c, "lists concat");
+        {
+            const uint32_t* in3[3] = {B.m2l_cp, B.p2p_cp, nullptr};
+            uint32_t* out3[3] = {B.m2l_cpo, B.p2p_cpo, nullptr};
+            uint32_t* tot3[3] = {(uint32_t*)(info + INFO_MOVED_M2L), (uint32_t*)(info + INFO_MOVED_P2P), nullptr};
+            NB_TRY(nb_scan3_u32(c, in3, out3, nn + 1, tot3));
+        }
+        k_lv_move<<<sms * 8, 256, 0, c->st>>>(B);
+        NB_LAUNCHED(c, "lists move");
         c->launches += 2;
         // near-field work plan
         NB_TRY(nb_grow(c, c->p2p_nch, sizeof(uint32_t) * (nl + 1)));
@@ -406,8 +469,9 @@ int nb_build_lists(nbody_ctx* c) {
         NB_CU(c, cudaMemcpyAsync(c->h_stats, c->stats.p, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                  c->st));
         NB_CU(c, cudaStreamSynchronize(c->st));
-        c->h_stats[0] = (uint32_t)c->h_info[INFO_M2L_TAIL];
-        c->h_stats[2] = (uint32_t)c->h_info[INFO_P2P_TAIL];
+        // extent of each list buffer (staged entries plus the moved ones)
+        c->h_info[INFO_M2L_TAIL] = c->h_info[INFO_BASE_M2L] + c->h_info[INFO_LVL_M2L] + c->h_info[INFO_MOVED_M2L];
+        c->h_info[INFO_P2P_TAIL] = c->h_info[INFO_BASE_P2P] + c->h_info[INFO_LVL_P2P] + c->h_info[INFO_MOVED_P2P];
         const uint32_t e = (uint32_t)c->h_info[INFO_ERR];
         const uint32_t caps = NB_ERRBIT_PEND_CAP | NB_ERRBIT_P2P_CAP | NB_ERRBIT_M2L_CAP | NB_ERRBIT_ITEM_CAP;
         if (!(e & caps)) return NBODY_OK;

@@ -42,7 +42,10 @@ enum {
     INFO_LVL_PEND = 35,            // pending entries written by the current level
     INFO_BASE_M2L = 36,            // staged far-field entries of the levels before
     INFO_BASE_P2P = 37,            // staged near-field entries of the levels before
-    INFO_WORDS = 40
+    INFO_MOVED_M2L = 38,           // far-field entries moved behind the staged ones
+    INFO_MOVED_P2P = 39,           // near-field entries moved behind the staged ones
+    INFO_ITEMS1 = 40,              // list-building items of the current level plus one (scan length)
+    INFO_WORDS = 48
 };
 
 // one octree node, breadth-first order, 32 bytes
@@ -95,8 +98,7 @@ struct nbody_ctx {
     DevBuf M, M32, L, src;
     DevBuf pend_off, pend_cnt, pend_list;          // pending lists, two level parities
     DevBuf p2p_off, p2p_cnt, p2p_list, m2l_off, m2l_cnt, m2l_list;   // per-target lists
-    DevBuf p2p_stage, m2l_stage;                    // per-level blocks before concatenation
-    DevBuf lst_seg, lst_nch, lst_first, lst_target, lst_cnt, lst_off;   // list-building work
+    DevBuf lst_seg, lst_nch, lst_first, lst_target, lst_cnt, lst_off, lst_cp;   // list-building work
     size_t pend_cap = 0, p2p_cap = 0, m2l_cap = 0, item_cap = 0;
     DevBuf stage;                  // host <-> device staging (interleaved doubles)
     DevBuf diag;
@@ -147,8 +149,10 @@ static inline T* DP(const DevBuf& b) { return reinterpret_cast<T*>(b.p); }
 
 // scan + sort (sort.cu)
 int nb_scan_u32(nbody_ctx* c, const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total_dev);
+// up to three exclusive scans in one set of launches (null inputs skipped); with n_dev, only the
+// first *n_dev of the n entries are scanned
 int nb_scan3_u32(nbody_ctx* c, const uint32_t* const in[3], uint32_t* const out[3], int64_t n,
-                 uint32_t* const total_dev[3]);
+                 uint32_t* const total_dev[3], const uint32_t* n_dev = nullptr);
 int nb_radix_sort(nbody_ctx* c, int64_t n, uint64_t* k0, uint32_t* v0, uint64_t* k1, uint32_t* v1, int begin_bit,
                   int end_bit, int* result_in_first);
 

@@ -80,17 +80,30 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const uint32_t* __re
 
 // the same three phases over K arrays at once (one launch per phase for all of them)
 struct ScanK {
-    const uint32_t* in[3];
+    const uint32_t* in[3];         // null: array unused
     uint32_t* out[3];
     uint32_t* total[3];
+    const uint32_t* n_dev;         // non-null: scan only the first *n_dev entries (<= n)
 };
+
+__device__ __forceinline__ int64_t scan_len(const ScanK& A, int64_t n) {
+    if (!A.n_dev) return n;
+    const int64_t m = (int64_t)*A.n_dev;
+    return m < n ? m : n;
+}
 
 template <int K>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scank_reduce(ScanK A, int64_t n, uint32_t* __restrict__ part,
                                                                  int64_t nb) {
+    n = scan_len(A, n);
     const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    if ((int64_t)blockIdx.x * SCAN_TILE >= n) {
+        if (threadIdx.x < K) part[threadIdx.x * nb + blockIdx.x] = 0;
+        return;
+    }
 #pragma unroll
     for (int a = 0; a < K; ++a) {
+        if (!A.in[a]) continue;
         uint32_t s = 0;
 #pragma unroll
         for (int k = 0; k < SCAN_ITEMS; ++k)
@@ -105,6 +118,7 @@ template <int K>
 __global__ void __launch_bounds__(1024) k_scank_partials(ScanK A, uint32_t* part, int64_t nb) {
 #pragma unroll
     for (int a = 0; a < K; ++a) {
+        if (!A.in[a]) continue;
         uint32_t run = 0;
         for (int64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
             const int64_t i = b0 + threadIdx.x;
@@ -121,9 +135,12 @@ __global__ void __launch_bounds__(1024) k_scank_partials(ScanK A, uint32_t* part
 template <int K>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scank_down(ScanK A, int64_t n, const uint32_t* __restrict__ part,
                                                                int64_t nb) {
+    n = scan_len(A, n);
+    if ((int64_t)blockIdx.x * SCAN_TILE >= n) return;
     const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
 #pragma unroll
     for (int a = 0; a < K; ++a) {
+        if (!A.in[a]) continue;
         uint32_t v[SCAN_ITEMS];
         uint32_t s = 0;
 #pragma unroll
@@ -218,7 +235,7 @@ int nb_scan_u32(nbody_ctx* c, const uint32_t* in, uint32_t* out, int64_t n, uint
 }
 
 int nb_scan3_u32(nbody_ctx* c, const uint32_t* const in[3], uint32_t* const out[3], int64_t n,
-                 uint32_t* const total_dev[3]) {
+                 uint32_t* const total_dev[3], const uint32_t* n_dev) {
     if (n <= 0) {
         for (int a = 0; a < 3; ++a)
             if (total_dev[a]) NB_CU(c, cudaMemsetAsync(total_dev[a], 0, sizeof(uint32_t), c->st));
@@ -229,6 +246,7 @@ int nb_scan3_u32(nbody_ctx* c, const uint32_t* const in[3], uint32_t* const out[
     uint32_t* part = DP<uint32_t>(c->scan_part);
     ScanK A;
     for (int a = 0; a < 3; ++a) { A.in[a] = in[a]; A.out[a] = out[a]; A.total[a] = total_dev[a]; }
+    A.n_dev = n_dev;
     k_scank_reduce<3><<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(A, n, part, nb);
     k_scank_partials<3><<<1, 1024, 0, c->st>>>(A, part, nb);
     k_scank_down<3><<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(A, n, part, nb);
