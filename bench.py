@@ -188,7 +188,8 @@ def main():
     ap.add_argument("--ref-targets", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--adj-steps", type=int, default=10, help="steps of the timed forward+adjoint run (0: skip)")
-    ap.add_argument("--adj-every", type=int, default=2, help="checkpoint spacing of the forward+adjoint run")
+    ap.add_argument("--adj-every", type=int, default=0,
+                    help="checkpoint spacing of the forward+adjoint run (0: every evaluation recorded)")
     a = ap.parse_args()
     assert a.warmup >= 0 and a.steps >= 1
     rank, world, local = dist_env()
@@ -304,9 +305,16 @@ def main():
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             adj_ms = float(t.item())
         fin = all(bool(torch.isfinite(t).all()) for t in out)
+        # phases of one force VJP at the final state
+        sim.set_timing(True)
+        mu = (wv * a.dt).cpu().numpy()
+        sim.force_vjp(mu)
+        vjp_ph = {k: float(v) for k, v in zip(nb.CudaSimulation.VJP_PHASES, sim.vjp_phase_times())}
+        vjp_launches = sim.stats()["launches"]
+        sim.set_timing(False)
         fwd_adj = {"value": a.n * a.adj_steps * world / (adj_ms * 1e-3), "unit": UNIT,
                    "ms_per_step": adj_ms / a.adj_steps, "steps": a.adj_steps, "checkpoint_every": a.adj_every,
-                   "gradients_finite": fin,
+                   "gradients_finite": fin, "vjp_phase_ms": vjp_ph, "vjp_launches": vjp_launches,
                    "note": "one recorded leapfrog run of `steps` steps plus its reverse sweep (frozen-tree "
                            "discrete adjoint: one force VJP per time point, re-evaluation from snapshots); "
                            "loss sum(wx . x_N + wv . v_N), seeds and gradients resident on the device"}

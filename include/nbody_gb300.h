@@ -114,13 +114,18 @@ int nbody_compute_forces(nbody_ctx* c, double* acc, double* pot);
    G/m_i mu_i . E_i (its acceleration does not carry E_i). */
 int nbody_force_vjp(nbody_ctx* c, const double* mu, double* gx, double* gq, double* gm);
 
-/* Advances nsteps leapfrog (KDK) steps like nbody_step, recording the sorted
-   state every `every` steps (plus the final state) for nbody_backward.  Device
-   memory: (ceil(nsteps / every) + every) snapshots of about 92 bytes per
-   particle in the FP64 and mixed forms, 48 in FP32.  every = 1 or 2 costs one
-   extra force evaluation per step in the reverse sweep; larger spacings
-   recompute the steps in between (about (2 every - 2) / every evaluations per
-   step). */
+/* Advances nsteps leapfrog (KDK) steps like nbody_step, recording for
+   nbody_backward.
+   every >= 1: the sorted state every `every` steps (plus the final state):
+   (ceil(nsteps / every) + every) snapshots of about 92 bytes per particle in
+   the FP64 and mixed forms, 48 in FP32.  The reverse sweep re-evaluates each
+   time point's tree and far field from its snapshot (the near field is not
+   needed: snapshots hold the accelerations); with every > 1 it also
+   recomputes the every - 1 full steps inside each checkpoint interval.
+   every = 0: every time point's whole evaluation (tree, lists, local
+   expansions, particle offsets), so the reverse sweep evaluates nothing:
+   about 370 bytes per particle per time point at order 5 and leaf capacity
+   64 (most of it the far-field lists), plus one state snapshot. */
 int nbody_forward_checkpointed(nbody_ctx* c, int nsteps, int every, double* t_out);
 
 /* Reverse sweep of the run recorded by the last nbody_forward_checkpointed:
@@ -196,8 +201,10 @@ int nbody_get_interactions(nbody_ctx* c, int which, int64_t* npairs, int32_t* pa
 
 /* Per-phase device times (ms) of the last force evaluation: 0 kick/drift +
    keys, 1 sort + gather, 2 tree, 3 upward pass (P2M, M2M), 4 interaction
-   lists, 5 far field (M2L, L2L), 6 near field + L2P + integration.  Timing
-   is enabled by nbody_set_timing(c, 1). */
+   lists, 5 far field (M2L, L2L), 6 near field + L2P + integration; and of the
+   last nbody_force_vjp: 7 adjoint seeds + L2P transpose, 8 L2L transpose,
+   9 M2L transpose, 10 M2M transpose, 11 near field + P2M/L2P adjoints.
+   n <= 12.  Timing is enabled by nbody_set_timing(c, 1). */
 int nbody_set_timing(nbody_ctx* c, int on);
 int nbody_phase_times(nbody_ctx* c, float* ms, int n);
 

@@ -76,6 +76,7 @@ int snap_load(nbody_ctx* c, int slot) {
         NB_CU(c, cudaMemcpyAsync(arr[i]->p, base + i * rb, rb, cudaMemcpyDeviceToDevice, c->st));
     NB_CU(c, cudaMemcpyAsync(id->p, base + 11 * rb, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToDevice, c->st));
     c->have_acc = true;
+    c->eval_current = false;
     return NBODY_OK;
 }
 
@@ -128,10 +129,91 @@ int rev_drift(nbody_ctx* c) {
     return NBODY_OK;
 }
 
+// evaluation records: the buffers the force VJP reads, with their sizes for a given tree
+struct RecField {
+    DevBuf* buf;
+    size_t bytes;
+};
+
+int rec_fields(nbody_ctx* c, int64_t nn, int64_t nl, uint32_t m2l_ext, uint32_t p2p_ext, RecField* f) {
+    const int64_t n = c->n;
+    const int k = c->cur;
+    const int p = c->prm.order;
+    const size_t terms = (size_t)(p + 1) * (p + 2) * (p + 3) / 6;
+    const size_t s4 = c->prm.precision == NBODY_PREC_FP64 ? 32 : 16;
+    const size_t hs = c->prm.precision == NBODY_PREC_FP32 ? 4 : 8;
+    int i = 0;
+    f[i++] = {&c->nodes, sizeof(NodeRec) * (size_t)nn};
+    f[i++] = {&c->leaves, sizeof(uint32_t) * (size_t)nl};
+    f[i++] = {&c->box, sizeof(BoxDev)};
+    f[i++] = {&c->src, s4 * (size_t)n};
+    f[i++] = {&c->id[k], sizeof(uint32_t) * (size_t)n};
+    for (DevBuf* b : {&c->q[k], &c->m[k], &c->ax[k], &c->ay[k], &c->az[k]}) f[i++] = {b, c->rsz * (size_t)n};
+    f[i++] = {&c->L, hs * terms * (size_t)nn};
+    f[i++] = {&c->m2l_off, sizeof(uint32_t) * (size_t)nn};
+    f[i++] = {&c->m2l_cnt, sizeof(uint32_t) * (size_t)nn};
+    f[i++] = {&c->m2l_list, sizeof(uint32_t) * (size_t)m2l_ext};
+    f[i++] = {&c->p2p_off, sizeof(uint32_t) * (size_t)nn};
+    f[i++] = {&c->p2p_cnt, sizeof(uint32_t) * (size_t)nn};
+    f[i++] = {&c->p2p_list, sizeof(uint32_t) * (size_t)p2p_ext};
+    f[i++] = {&c->p2p_work_off, sizeof(uint32_t) * (size_t)(nl + 1)};
+    f[i++] = {&c->p2p_part_off, sizeof(uint32_t) * (size_t)(nl + 1)};
+    return i;
+}
+
+inline size_t al256(size_t b) { return (b + 255) / 256 * 256; }
+
+// records the current evaluation as record j
+int rec_save(nbody_ctx* c, int j) {
+    if ((int)c->recs.size() <= j) c->recs.resize(j + 1);
+    EvalRecord& R = c->recs[j];
+    RecField f[24];
+    const int nf = rec_fields(c, c->nnodes, c->nleaves, (uint32_t)c->h_info[INFO_M2L_TAIL],
+                              (uint32_t)c->h_info[INFO_P2P_TAIL], f);
+    size_t total = 0;
+    for (int i = 0; i < nf; ++i) total += al256(f[i].bytes);
+    NB_TRY(nb_grow(c, R.buf, total));
+    size_t o = 0;
+    for (int i = 0; i < nf; ++i) {
+        if (f[i].bytes)
+            NB_CU(c, cudaMemcpyAsync((char*)R.buf.p + o, f[i].buf->p, f[i].bytes, cudaMemcpyDeviceToDevice, c->st));
+        o += al256(f[i].bytes);
+    }
+    R.nn = c->nnodes;
+    R.nl = c->nleaves;
+    R.depth = c->depth;
+    std::copy(c->level_start, c->level_start + NB_LEVELS + 3, R.level_start);
+    std::copy(c->h_info, c->h_info + INFO_WORDS, R.info);
+    return NBODY_OK;
+}
+
+// makes record j the context's current evaluation (the particle state arrays it includes are the
+// sorted charges, masses, accelerations and ids; positions and velocities are left alone)
+int rec_load(nbody_ctx* c, int j) {
+    EvalRecord& R = c->recs[j];
+    RecField f[24];
+    const int nf = rec_fields(c, R.nn, R.nl, (uint32_t)R.info[INFO_M2L_TAIL], (uint32_t)R.info[INFO_P2P_TAIL], f);
+    size_t o = 0;
+    for (int i = 0; i < nf; ++i) {
+        NB_TRY(nb_grow(c, *f[i].buf, f[i].bytes));
+        if (f[i].bytes)
+            NB_CU(c, cudaMemcpyAsync(f[i].buf->p, (const char*)R.buf.p + o, f[i].bytes, cudaMemcpyDeviceToDevice, c->st));
+        o += al256(f[i].bytes);
+    }
+    c->nnodes = R.nn;
+    c->nleaves = R.nl;
+    c->depth = R.depth;
+    std::copy(R.level_start, R.level_start + NB_LEVELS + 3, c->level_start);
+    std::copy(R.info, R.info + INFO_WORDS, c->h_info);
+    const int64_t npart = (uint32_t)R.info[INFO_P2P_PART];
+    NB_TRY(nb_grow(c, c->p2p_part, c->rsz * 4 * (size_t)(npart + 1)));
+    return NBODY_OK;
+}
+
 // snapshot slots: 0 .. nck-1 checkpoints, then `every - 1` segment slots, then the final state
-int nck(const nbody_ctx* c) { return (c->ck_steps + c->ck_every - 1) / c->ck_every; }
+int nck(const nbody_ctx* c) { return c->rec_mode ? 0 : (c->ck_steps + c->ck_every - 1) / c->ck_every; }
 int seg_slot(const nbody_ctx* c, int j) { return nck(c) + j; }
-int final_slot(const nbody_ctx* c) { return nck(c) + c->ck_every - 1; }
+int final_slot(const nbody_ctx* c) { return c->rec_mode ? 0 : nck(c) + c->ck_every - 1; }
 
 }  // namespace
 
@@ -167,26 +249,31 @@ int nbody_forward_checkpointed(nbody_ctx* c, int nsteps, int every, double* t_ou
     if (c->n == 0) return nb_fail(c, NBODY_ERR_STATE, "no particles");
     if (c->prm.integrator != NBODY_INTEG_LEAPFROG)
         return nb_fail(c, NBODY_ERR_INVALID, "the recorded run needs the leapfrog integrator");
-    if (nsteps < 1 || every < 1) return nb_fail(c, NBODY_ERR_INVALID, "nsteps and every must be >= 1");
+    if (nsteps < 1 || every < 0) return nb_fail(c, NBODY_ERR_INVALID, "nsteps must be >= 1 and every >= 0");
     NB_CU(c, cudaSetDevice(c->device));
-    every = std::min(every, nsteps);
+    const bool rec = every == 0;
+    every = rec ? 1 : std::min(every, nsteps);
     c->ck_steps = 0;
+    c->rec_mode = rec;
     c->snap_bytes = snapshot_bytes(c);
-    const int slots = (nsteps + every - 1) / every + every;
+    const int slots = rec ? 1 : (nsteps + every - 1) / every + every;
     NB_TRY(nb_grow(c, c->snaps, c->snap_bytes * (size_t)slots));
-    if (!c->have_acc) {
+    // time point 0 needs its accelerations, and in record mode its whole evaluation
+    if (!c->have_acc || (rec && !c->eval_current)) {
         NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
         c->have_acc = true;
     }
     c->ck_t0 = c->time;
     c->ck_every = every;
     c->ck_steps = nsteps;
-    NB_TRY(snap_save(c, 0));
+    if (rec) NB_TRY(rec_save(c, 0));
+    else NB_TRY(snap_save(c, 0));
     for (int s = 0; s < nsteps; ++s) {
         NB_TRY(nb_evaluate(c, 1, NB_INTEG_KDK_CLOSE, false));
         c->time += c->prm.dt;
         const int pt = s + 1;
-        if (pt < nsteps && pt % every == 0) NB_TRY(snap_save(c, pt / every));
+        if (rec) NB_TRY(rec_save(c, pt));
+        else if (pt < nsteps && pt % every == 0) NB_TRY(snap_save(c, pt / every));
     }
     NB_TRY(snap_save(c, final_slot(c)));
     NB_CU(c, cudaStreamSynchronize(c->st));
@@ -209,6 +296,26 @@ int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* g
     NB_TRY(upload_r(c, gvT, 3 * n, c->adj_lv, st + 3 * n));
     NB_CU(c, cudaMemsetAsync(c->adj_gq.p, 0, c->rsz * n, c->st));
     NB_CU(c, cudaMemsetAsync(c->adj_gm.p, 0, c->rsz * n, c->st));
+    if (c->rec_mode) {
+        // every time point's evaluation was recorded: no re-evaluation
+        for (int pt = N; pt >= 0; --pt) {
+            if (pt < N) NB_TRY(rev_drift(c));
+            if (pt < N || !c->tree_at_final) NB_TRY(rec_load(c, pt));
+            NB_TRY(vjp(c, pt == N || pt == 0 ? 0.5 * dt : dt));
+        }
+        NB_TRY(download_r(c, c->adj_lx, 3 * n, gx0, st));
+        NB_TRY(download_r(c, c->adj_lv, 3 * n, gv0, st + 3 * n));
+        NB_TRY(download_r(c, c->adj_gq, n, gq, st + 6 * n));
+        NB_TRY(download_r(c, c->adj_gm, n, gm, st + 7 * n));
+        // back to the final state with its evaluation current
+        NB_TRY(snap_load(c, final_slot(c)));
+        NB_TRY(rec_load(c, N));
+        c->eval_current = true;
+        c->tree_at_final = true;
+        c->time = c->ck_t0 + N * dt;
+        NB_CU(c, cudaStreamSynchronize(c->st));
+        return NBODY_OK;
+    }
     // time point N
     if (!c->tree_at_final) {
         NB_TRY(snap_load(c, final_slot(c)));

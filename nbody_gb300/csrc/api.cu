@@ -179,6 +179,7 @@ int fmm(nbody_ctx* c, int integ, bool want_pot) {
 int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
     c->launches = 0;
     c->tree_at_final = false;
+    c->eval_current = false;
     if (c->timing) cudaEventRecord(c->ev[0], c->st);
     NB_TRY(nb_begin_step(c, kdk));
     if (c->timing) cudaEventRecord(c->ev[1], c->st);
@@ -195,6 +196,7 @@ int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
         NB_CU(c, cudaEventSynchronize(c->ev[7]));
         for (int i = 0; i < 7; ++i) cudaEventElapsedTime(&c->phase_ms[i], c->ev[i], c->ev[i + 1]);
     }
+    c->eval_current = true;
     return NBODY_OK;
 }
 
@@ -297,6 +299,7 @@ int nbody_destroy(nbody_ctx* c) {
                       &c->snaps, &c->lst_seg, &c->lst_nch, &c->lst_first, &c->lst_target, &c->lst_cnt,
                       &c->lst_off, &c->lst_cp})
         release(*b);
+    for (EvalRecord& r : c->recs) release(r.buf);
     if (c->h_info) cudaFreeHost(c->h_info);
     for (int i = 0; i < 16; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
@@ -339,6 +342,7 @@ int nbody_set_state(nbody_ctx* c, int64_t n, const double* pos, const double* ve
     c->time = 0.0;
     c->have_acc = acc != nullptr;
     c->ck_steps = 0;
+    c->eval_current = false;
     return NBODY_OK;
 }
 

@@ -71,6 +71,16 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+// one recorded force evaluation: everything the force VJP reads (tree, lists, local expansions,
+// particle offsets, sorted charges/masses/accelerations/ids), packed in one device block
+struct EvalRecord {
+    DevBuf buf;
+    int64_t nn = 0, nl = 0;
+    int depth = 0;
+    int level_start[NB_LEVELS + 3] = {0};
+    int32_t info[INFO_WORDS] = {0};
+};
+
 struct nbody_ctx {
     nbody_params prm;
     int device = 0;
@@ -120,6 +130,9 @@ struct nbody_ctx {
     int ck_every = 0;              // checkpoint spacing of the recorded run
     double ck_t0 = 0.0;            // simulated time at its start
     bool tree_at_final = false;    // the last evaluation was the recorded run's final one
+    bool rec_mode = false;         // the recorded run kept every evaluation (no re-evaluation backward)
+    bool eval_current = false;     // tree, lists and expansions match the current state
+    std::vector<EvalRecord> recs;  // its evaluations, time points 0 .. steps
 
     // per-phase timing
     bool timing = false;

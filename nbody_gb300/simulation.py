@@ -208,7 +208,8 @@ class CudaSimulation:
         return gx, gq, gm
 
     def forward_checkpointed(self, nsteps: int, every: int = 1) -> float:
-        """nsteps leapfrog steps, recording snapshots every `every` steps for backward()."""
+        """nsteps leapfrog steps recorded for backward(): snapshots every `every` steps, or with every = 0
+        every time point's whole evaluation (no re-evaluation in the reverse sweep)."""
         t = C.c_double()
         check(self._h, _lib.load().nbody_forward_checkpointed(self._h, int(nsteps), int(every), C.byref(t)))
         return t.value

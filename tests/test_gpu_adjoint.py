@@ -8,7 +8,8 @@ Checks
                                 order 8 FP64 3e-6, order 5 mixed 3e-4 relative rms
   trajectory adjoint          vs the FP64 direct-sum leapfrog adjoint (oracle),
                                 order 8 FP64, 1e-6 relative
-  checkpoint spacing          every = 1, 2, 3, N give bitwise identical gradients
+  checkpoint spacing          every = 1, 2, 3, N and recorded evaluations (0) give bitwise
+                                identical gradients
   state after the reverse sweep is the recorded run's final state, bitwise
 """
 import numpy as np
@@ -127,7 +128,7 @@ def test_checkpoint_spacing_gives_identical_gradients(nb, prec):
     rng = np.random.default_rng(9)
     gxT, gvT = rng.normal(size=pos.shape), rng.normal(size=pos.shape)
     ref, _ = _run(nb, pos, vel, m, prec, 5, 7, 1, gxT, gvT)
-    for every in (2, 3, 7):
+    for every in (0, 2, 3, 7):
         g, _ = _run(nb, pos, vel, m, prec, 5, 7, every, gxT, gvT)
         for a, b in zip(g, ref):
             np.testing.assert_array_equal(a, b)
