@@ -21,6 +21,8 @@
 // reproducible run to run.
 #pragma once
 
+#include <type_traits>
+
 #include "nbody_internal.cuh"
 #include "fmm_ops.inc"
 
@@ -499,11 +501,31 @@ __device__ __forceinline__ void p2p_epilogue(const P2PArgs& A, uint32_t i, const
     if (pot) ((R*)A.pot)[i] = -(R)A.G * Ps;
 }
 
-// One warp's share of a near-field work item: every target of the leaf
-// (two per lane, CT lanes per group) against the partner leaves
-// [s_lo, s_hi) of its list.  GUARD: unsoftened kernel, so r = 0 must give 0.
-template <int MODE, int P, bool POT, bool GUARD>
-__device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::S4 (*tile)[P2P_TILE],
+// lanes per target group and targets per lane of near-field class CLS (see nb_p2p_class)
+template <int CLS> struct P2PShape;
+template <> struct P2PShape<0> { static constexpr int CT = 4, TPL = 2; };
+template <> struct P2PShape<1> { static constexpr int CT = 8, TPL = 2; };
+template <> struct P2PShape<2> { static constexpr int CT = 8, TPL = 3; };
+template <> struct P2PShape<3> { static constexpr int CT = 16, TPL = 2; };
+template <> struct P2PShape<4> { static constexpr int CT = 16, TPL = 3; };
+template <> struct P2PShape<5> { static constexpr int CT = 32, TPL = 2; };
+constexpr int P2P_WTILE = 128;    // shared source entries per warp (groups x entries per group)
+
+// which leaf / chunk a near-field work item is: last li in [lo, hi) with work_off[li] <= w
+__device__ __forceinline__ int64_t p2p_leaf_of(const uint32_t* work_off, int64_t lo, int64_t hi, uint32_t w) {
+    while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (work_off[mid] <= w) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// One warp's share of a near-field work item: every target of the leaf (TPL per lane, CT lanes per
+// group) against the partner leaves [s_lo, s_hi) of its list.  NG = 32/CT groups take partner
+// leaves round-robin; each group's source tile (TILE entries) is prefetched into registers while
+// the previous one is evaluated from shared memory.  GUARD: unsoftened kernel, r = 0 gives 0.
+template <int MODE, int P, bool POT, bool GUARD, int CT, int TPL>
+__device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::S4* tile,
                                          const typename Prec<MODE>::S* sL, uint32_t k, const NodeRec& nt,
                                          int64_t li, uint32_t chunk, uint32_t nchunk, uint32_t s_lo,
                                          uint32_t s_hi) {
@@ -511,23 +533,33 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
     typedef typename Prec<MODE>::S S;
     typedef typename Prec<MODE>::S4 S4;
     constexpr bool KH = Prec<MODE>::kahan;
+    constexpr int NG = 32 / CT;
+    constexpr int TILE = P2P_WTILE / NG < 32 ? P2P_WTILE / NG : 32;
+    constexpr int EPL = TILE / CT;          // tile entries each lane loads
     const int lane = lane_id();
+    const int grp = lane / CT, gl = lane % CT;
+    S4* gtile = tile + grp * TILE;
     const double unit = A.box->unit;
     const S4* src = (const S4*)A.src;
     const uint32_t cnt_t = nt.count;
-    const int CT = cnt_t <= 16 ? 8 : cnt_t <= 32 ? 16 : 32;
-    const int NG = 32 / CT, grp = lane / CT, gl = lane % CT, TPL = P2P_TILE / CT;
     const uint32_t loff = A.p2p_off[k];
     const S eps2 = (S)A.eps2;
     S4 zero4;
     zero4.x = 0; zero4.y = 0; zero4.z = 0; zero4.w = 0;
-    for (uint32_t tc = 0; tc < cnt_t; tc += 2 * CT) {
-        const uint32_t ta = tc + gl, tb = tc + CT + gl;
-        const bool va = ta < cnt_t, vb = tb < cnt_t;
-        const uint32_t ia = nt.begin + (va ? ta : 0), ib = nt.begin + (vb ? tb : 0);
-        const S4 ya = src[ia], yb = src[ib];
-        S ax = 0, ay = 0, az = 0, ap = 0, bx = 0, by = 0, bz = 0, bp = 0;
-        S cax = 0, cay = 0, caz = 0, cap = 0, cbx = 0, cby = 0, cbz = 0, cbp = 0;
+    for (uint32_t tc = 0; tc < cnt_t; tc += TPL * CT) {
+        uint32_t ti[TPL], ii[TPL];
+        bool tv[TPL];
+        S4 y[TPL];
+        S acc[TPL][4], cmp[TPL][4];
+#pragma unroll
+        for (int j = 0; j < TPL; ++j) {
+            ti[j] = tc + gl + j * CT;
+            tv[j] = ti[j] < cnt_t;
+            ii[j] = nt.begin + (tv[j] ? ti[j] : 0);
+            y[j] = src[ii[j]];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) { acc[j][q] = 0; cmp[j][q] = 0; }
+        }
         for (uint32_t base = s_lo; base < s_hi; base += 32) {
             const uint32_t nb = min(32u, s_hi - base);
             uint32_t my_s = 0, my_beg = 0, my_cnt = 0;
@@ -555,14 +587,16 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
             }
             const uint32_t rounds = (nb + NG - 1) / NG;
             uint32_t rr = 0, sb = 0;
-            const uint32_t cur_beg = __shfl_sync(0xffffffffu, my_beg, grp);
-            const uint32_t cur_cnt0 = __shfl_sync(0xffffffffu, my_cnt, grp);
-            const uint32_t cur_cnt = (uint32_t)grp < nb ? cur_cnt0 : 0u;
-            S4 pre[4];
+            S4 pre[EPL];
+            {
+                const uint32_t cbeg = __shfl_sync(0xffffffffu, my_beg, grp);
+                const uint32_t ccnt0 = __shfl_sync(0xffffffffu, my_cnt, grp);
+                const uint32_t ccnt = (uint32_t)grp < nb ? ccnt0 : 0u;
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const uint32_t j = sb + gl + e * CT;
-                pre[e] = (e < TPL && j < cur_cnt) ? src[cur_beg + j] : zero4;
+                for (int e = 0; e < EPL; ++e) {
+                    const uint32_t j = gl + e * CT;
+                    pre[e] = j < ccnt ? src[cbeg + j] : zero4;
+                }
             }
             while (rr < rounds) {
                 const uint32_t q = rr * NG + grp;
@@ -576,10 +610,9 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
 #pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    if (e < TPL) tile[grp][gl + e * CT] = pre[e];
+                for (int e = 0; e < EPL; ++e) gtile[gl + e * CT] = pre[e];
                 __syncwarp();
-                uint32_t nrr = rr, nsb = sb + P2P_TILE;
+                uint32_t nrr = rr, nsb = sb + TILE;
                 if (nsb >= mx) { nrr = rr + 1; nsb = 0; }
                 {
                     const uint32_t nq = nrr * NG + grp;
@@ -587,86 +620,94 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
                     const uint32_t ncnt0 = __shfl_sync(0xffffffffu, my_cnt, nq & 31);
                     const uint32_t ncnt = (nrr < rounds && nq < nb) ? ncnt0 : 0u;
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) {
+                    for (int e = 0; e < EPL; ++e) {
                         const uint32_t j = nsb + gl + e * CT;
-                        pre[e] = (e < TPL && j < ncnt) ? src[nbeg + j] : zero4;
+                        pre[e] = j < ncnt ? src[nbeg + j] : zero4;
                     }
                 }
-                // both targets, shifted into the source leaf's frame
-                const S xa = ya.x - dx, ya_ = ya.y - dy, za = ya.z - dz;
-                const S xb = yb.x - dx, yb_ = yb.y - dy, zb = yb.z - dz;
-                const int nj = scnt > sb ? min((int)(scnt - sb), P2P_TILE) : 0;
-                S pax = 0, pay = 0, paz = 0, pap = 0, pbx = 0, pby = 0, pbz = 0, pbp = 0;
+                // targets shifted into the source leaf's frame
+                S xs[TPL][3];
+#pragma unroll
+                for (int j = 0; j < TPL; ++j) { xs[j][0] = y[j].x - dx; xs[j][1] = y[j].y - dy; xs[j][2] = y[j].z - dz; }
+                const int nj = scnt > sb ? min((int)(scnt - sb), TILE) : 0;
+                const bool self = POT && s_id == k;
+                S p[TPL][4];
+#pragma unroll
+                for (int j = 0; j < TPL; ++j) { p[j][0] = 0; p[j][1] = 0; p[j][2] = 0; p[j][3] = 0; }
 #pragma unroll 2
                 for (int e = 0; e < nj; ++e) {
-                    const S4 sj = tile[grp][e];
-                    const S rxa = sj.x - xa, rya = sj.y - ya_, rza = sj.z - za;
-                    const S rxb = sj.x - xb, ryb = sj.y - yb_, rzb = sj.z - zb;
-                    S s2a = nb_fma(rxa, rxa, nb_fma(rya, rya, nb_fma(rza, rza, eps2)));
-                    S s2b = nb_fma(rxb, rxb, nb_fma(ryb, ryb, nb_fma(rzb, rzb, eps2)));
-                    if (GUARD) { s2a = s2a > S(0) ? s2a : S(1e30); s2b = s2b > S(0) ? s2b : S(1e30); }
-                    S inva = nb_rsqrt(s2a), invb = nb_rsqrt(s2b);
-                    if (POT && s_id == k && sb + e == ta) inva = S(0);
-                    if (POT && s_id == k && sb + e == tb) invb = S(0);
-                    const S wa = sj.w * inva * inva * inva, wb = sj.w * invb * invb * invb;
-                    pax = nb_fma(rxa, wa, pax); pay = nb_fma(rya, wa, pay); paz = nb_fma(rza, wa, paz);
-                    pbx = nb_fma(rxb, wb, pbx); pby = nb_fma(ryb, wb, pby); pbz = nb_fma(rzb, wb, pbz);
-                    if (POT) { pap = nb_fma(sj.w, inva, pap); pbp = nb_fma(sj.w, invb, pbp); }
+                    const S4 sj = gtile[e];
+#pragma unroll
+                    for (int j = 0; j < TPL; ++j) {
+                        const S rx = sj.x - xs[j][0], ry = sj.y - xs[j][1], rz = sj.z - xs[j][2];
+                        S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
+                        if (GUARD) s2 = s2 > S(0) ? s2 : S(1e30);
+                        S inv = nb_rsqrt(s2);
+                        if (self && sb + e == ti[j]) inv = S(0);
+                        const S w = sj.w * inv * inv * inv;
+                        p[j][0] = nb_fma(rx, w, p[j][0]);
+                        p[j][1] = nb_fma(ry, w, p[j][1]);
+                        p[j][2] = nb_fma(rz, w, p[j][2]);
+                        if (POT) p[j][3] = nb_fma(sj.w, inv, p[j][3]);
+                    }
                 }
-                if (KH) {
-                    kahan_add(ax, cax, pax); kahan_add(ay, cay, pay); kahan_add(az, caz, paz);
-                    kahan_add(bx, cbx, pbx); kahan_add(by, cby, pby); kahan_add(bz, cbz, pbz);
-                    if (POT) { kahan_add(ap, cap, pap); kahan_add(bp, cbp, pbp); }
-                } else {
-                    ax += pax; ay += pay; az += paz; bx += pbx; by += pby; bz += pbz;
-                    if (POT) { ap += pap; bp += pbp; }
-                }
+#pragma unroll
+                for (int j = 0; j < TPL; ++j)
+#pragma unroll
+                    for (int q = 0; q < (POT ? 4 : 3); ++q) {
+                        if (KH) kahan_add(acc[j][q], cmp[j][q], p[j][q]);
+                        else acc[j][q] += p[j][q];
+                    }
                 __syncwarp();
                 rr = nrr;
                 sb = nsb;
             }
         }
         // combine the source groups in a fixed order, in the state precision
-        R Ax = (R)ax - (R)cax, Ay = (R)ay - (R)cay, Az = (R)az - (R)caz, Ap = (R)ap - (R)cap;
-        R Bx = (R)bx - (R)cbx, By = (R)by - (R)cby, Bz = (R)bz - (R)cbz, Bp = (R)bp - (R)cbp;
+        R tot[TPL][4];
+#pragma unroll
+        for (int j = 0; j < TPL; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) tot[j][q] = (R)acc[j][q] - (R)cmp[j][q];
         for (int o = CT; o < 32; o <<= 1) {
-            Ax += shfl_xor_t(Ax, o); Ay += shfl_xor_t(Ay, o); Az += shfl_xor_t(Az, o);
-            Bx += shfl_xor_t(Bx, o); By += shfl_xor_t(By, o); Bz += shfl_xor_t(Bz, o);
-            if (POT) { Ap += shfl_xor_t(Ap, o); Bp += shfl_xor_t(Bp, o); }
+#pragma unroll
+            for (int j = 0; j < TPL; ++j)
+#pragma unroll
+                for (int q = 0; q < (POT ? 4 : 3); ++q) tot[j][q] += shfl_xor_t(tot[j][q], o);
         }
         if (grp == 0) {
-            if (nchunk == 1) {
-                if (va) p2p_epilogue<MODE, P>(A, ia, sL, ya, Ax, Ay, Az, Ap, POT);
-                if (vb) p2p_epilogue<MODE, P>(A, ib, sL, yb, Bx, By, Bz, Bp, POT);
-            } else {
-                R* pt = (R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)chunk * cnt_t);
-                if (va) { pt[4 * ta] = Ax; pt[4 * ta + 1] = Ay; pt[4 * ta + 2] = Az; pt[4 * ta + 3] = Ap; }
-                if (vb) { pt[4 * tb] = Bx; pt[4 * tb + 1] = By; pt[4 * tb + 2] = Bz; pt[4 * tb + 3] = Bp; }
+#pragma unroll
+            for (int j = 0; j < TPL; ++j) {
+                if (!tv[j]) continue;
+                if (nchunk == 1) {
+                    p2p_epilogue<MODE, P>(A, ii[j], sL, y[j], tot[j][0], tot[j][1], tot[j][2], tot[j][3], POT);
+                } else {
+                    R* pt = (R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)chunk * cnt_t + ti[j]);
+                    pt[0] = tot[j][0]; pt[1] = tot[j][1]; pt[2] = tot[j][2]; pt[3] = tot[j][3];
+                }
             }
         }
         __syncwarp();
     }
 }
 
-template <int MODE, int P, bool POT>
-__global__ void __launch_bounds__(32 * P2P_WARPS, 5) k_p2p(P2PArgs A) {
+// near-field work items of one leaf-size class: items [w_lo, w_hi) of leaves [li_lo, li_hi)
+template <int MODE, int P, bool POT, int CLS>
+__global__ void __launch_bounds__(32 * P2P_WARPS, P2PShape<CLS>::TPL == 3 ? 4 : 5) k_p2p(P2PArgs A, int64_t li_lo,
+                                                                                      int64_t li_hi, uint32_t w_lo,
+                                                                                      uint32_t w_hi) {
     typedef typename Prec<MODE>::S S;
     typedef typename Prec<MODE>::H H;
     typedef typename Prec<MODE>::S4 S4;
     constexpr int T = nb_terms<P>::value;
-    __shared__ S4 tile[P2P_WARPS][4][P2P_TILE];
+    constexpr int CT = P2PShape<CLS>::CT, TPL = P2PShape<CLS>::TPL;
+    __shared__ S4 tile[P2P_WARPS][P2P_WTILE];
     __shared__ S sL[P2P_WARPS][T];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
-    const int64_t w = (int64_t)blockIdx.x * P2P_WARPS + wib;
-    if (w >= A.nwork) return;
-    // which leaf / chunk: last li with work_off[li] <= w
-    int64_t lo = 0, hi = A.nleaves;
-    while (hi - lo > 1) {
-        const int64_t mid = (lo + hi) >> 1;
-        if (A.work_off[mid] <= (uint32_t)w) lo = mid; else hi = mid;
-    }
-    const int64_t li = lo;
-    const uint32_t chunk = (uint32_t)w - A.work_off[li];
+    const uint32_t w = w_lo + blockIdx.x * P2P_WARPS + wib;
+    if (w >= w_hi) return;
+    const int64_t li = p2p_leaf_of(A.work_off, li_lo, li_hi, w);
+    const uint32_t chunk = w - A.work_off[li];
     const uint32_t nchunk = A.work_off[li + 1] - A.work_off[li];
     const uint32_t k = A.leaves[li];
     const NodeRec nt = A.nodes[k];
@@ -677,8 +718,10 @@ __global__ void __launch_bounds__(32 * P2P_WARPS, 5) k_p2p(P2PArgs A) {
     const uint32_t lcnt = A.p2p_cnt[k];
     const uint32_t s_lo = chunk * P2P_CHUNK, s_hi = min(lcnt, s_lo + P2P_CHUNK);
     __syncwarp();
-    if (A.eps2 > 0.0) p2p_item<MODE, P, POT, false>(A, tile[wib], sL[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
-    else p2p_item<MODE, P, POT, true>(A, tile[wib], sL[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
+    if (A.eps2 > 0.0)
+        p2p_item<MODE, P, POT, false, CT, TPL>(A, tile[wib], sL[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
+    else
+        p2p_item<MODE, P, POT, true, CT, TPL>(A, tile[wib], sL[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
 }
 
 // sums the chunk partials of multi-chunk leaves in chunk order, then L2P + epilogue
@@ -715,6 +758,28 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p_final(P2PArgs A) {
 // ---------------------------------------------------------------------------
 // host driver for one (mode, order)
 // ---------------------------------------------------------------------------
+// one launch per non-empty leaf-size class, over that class's work items
+template <int MODE, int P, bool POT>
+int p2p_launch_classes(nbody_ctx* c, const P2PArgs& B) {
+    const int32_t* hi = c->h_info;
+    auto one = [&](auto cls_tag) -> int {
+        constexpr int CLS = decltype(cls_tag)::value;
+        const uint32_t w0 = (uint32_t)hi[INFO_CLS_WORK + CLS], w1 = (uint32_t)hi[INFO_CLS_WORK + CLS + 1];
+        if (w1 <= w0) return NBODY_OK;
+        const int64_t l0 = (uint32_t)hi[INFO_CLS_LEAF + CLS], l1 = (uint32_t)hi[INFO_CLS_LEAF + CLS + 1];
+        k_p2p<MODE, P, POT, CLS><<<(w1 - w0 + P2P_WARPS - 1) / P2P_WARPS, 32 * P2P_WARPS, 0, c->st>>>(B, l0, l1, w0, w1);
+        NB_LAUNCHED(c, "p2p");
+        c->launches += 1;
+        return NBODY_OK;
+    };
+    NB_TRY(one(std::integral_constant<int, 5>()));
+    NB_TRY(one(std::integral_constant<int, 4>()));
+    NB_TRY(one(std::integral_constant<int, 3>()));
+    NB_TRY(one(std::integral_constant<int, 2>()));
+    NB_TRY(one(std::integral_constant<int, 1>()));
+    NB_TRY(one(std::integral_constant<int, 0>()));
+    return NBODY_OK;
+}
 template <int MODE, int P>
 int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     typedef typename Prec<MODE>::R R;
@@ -807,17 +872,17 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     B.G = c->prm.G;
     B.dt = c->prm.dt;
     B.integ = integ;
-    const unsigned g = (unsigned)((nwork + P2P_WARPS - 1) / P2P_WARPS);
     const unsigned gf = (unsigned)((nl + P2P_WARPS - 1) / P2P_WARPS);
-    if (want_pot) {
-        k_p2p<MODE, P, true><<<g, 32 * P2P_WARPS, 0, c->st>>>(B);
-        if (npart) k_p2p_final<MODE, P, true><<<gf, 32 * P2P_WARPS, 0, c->st>>>(B);
-    } else {
-        k_p2p<MODE, P, false><<<g, 32 * P2P_WARPS, 0, c->st>>>(B);
-        if (npart) k_p2p_final<MODE, P, false><<<gf, 32 * P2P_WARPS, 0, c->st>>>(B);
+    {
+        const int rc = want_pot ? p2p_launch_classes<MODE, P, true>(c, B) : p2p_launch_classes<MODE, P, false>(c, B);
+        if (rc != NBODY_OK) return rc;
     }
-    NB_LAUNCHED(c, "p2p");
-    c->launches += npart ? 2 : 1;
+    if (npart) {
+        if (want_pot) k_p2p_final<MODE, P, true><<<gf, 32 * P2P_WARPS, 0, c->st>>>(B);
+        else k_p2p_final<MODE, P, false><<<gf, 32 * P2P_WARPS, 0, c->st>>>(B);
+        NB_LAUNCHED(c, "p2p final");
+        c->launches += 1;
+    }
     if (c->timing) cudaEventRecord(c->ev[7], c->st);
     return NBODY_OK;
 }

@@ -321,18 +321,44 @@ __global__ void k_lv_root(const NodeRec* nodes, uint32_t* pend_off, uint32_t* pe
     info[INFO_LVL_P2P] = leaf ? 1 : 0;
 }
 
-// near-field work plan: chunks of P2P_LEAF_CHUNK partner leaves per leaf and partial-sum slots
+// near-field work plan, per leaf (tree order): chunks of NB_P2P_CHUNK partner leaves, partial-sum
+// slots of split leaves, and the leaf's size class as the sort key
 __global__ void k_p2p_plan(int64_t nleaves, const uint32_t* __restrict__ leaves, const NodeRec* __restrict__ nodes,
                            const uint32_t* __restrict__ p2p_cnt, uint32_t* __restrict__ nch,
-                           uint32_t* __restrict__ psize) {
+                           uint32_t* __restrict__ psize, uint64_t* __restrict__ key, uint32_t* __restrict__ val) {
     const int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (li > nleaves) return;
-    if (li == nleaves) { nch[li] = 0; psize[li] = 0; return; }
+    if (li >= nleaves) return;
     const uint32_t k = leaves[li];
+    const uint32_t cnt = nodes[k].count;
     const uint32_t c = (p2p_cnt[k] + NB_P2P_CHUNK - 1) / NB_P2P_CHUNK;
     const uint32_t n = c > 1 ? c : 1u;
     nch[li] = n;
-    psize[li] = n > 1 ? n * nodes[k].count : 0u;
+    psize[li] = n > 1 ? n * cnt : 0u;
+    key[li] = (uint64_t)nb_p2p_class(cnt);
+    val[li] = (uint32_t)li;
+}
+
+// leaves regrouped by class (stable): new order, its chunk and slot counts, class boundaries
+__global__ void k_p2p_order(int64_t nleaves, const uint32_t* __restrict__ leaves_in, uint32_t* __restrict__ leaves_out,
+                            const uint32_t* __restrict__ nch_in, const uint32_t* __restrict__ psize_in,
+                            uint32_t* __restrict__ nch_out, uint32_t* __restrict__ psize_out,
+                            const uint64_t* __restrict__ key, const uint32_t* __restrict__ val, int32_t* info) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > nleaves) return;
+    if (j == nleaves) { nch_out[j] = 0; psize_out[j] = 0; return; }
+    const uint32_t o = val[j];
+    leaves_out[j] = leaves_in[o];
+    nch_out[j] = nch_in[o];
+    psize_out[j] = psize_in[o];
+    const int cl = (int)key[j], cp = j > 0 ? (int)key[j - 1] : -1;
+    for (int x = cp + 1; x <= cl; ++x) info[INFO_CLS_LEAF + x] = (int32_t)j;
+    if (j == nleaves - 1)
+        for (int x = cl + 1; x <= NB_P2P_CLASSES; ++x) info[INFO_CLS_LEAF + x] = (int32_t)nleaves;
+}
+
+__global__ void k_p2p_class_work(const uint32_t* __restrict__ work_off, int32_t* info) {
+    const int x = threadIdx.x;
+    if (x <= NB_P2P_CLASSES) info[INFO_CLS_WORK + x] = (int32_t)work_off[info[INFO_CLS_LEAF + x]];
 }
 
 }  // namespace
@@ -450,21 +476,41 @@ int nb_build_lists(nbody_ctx* c) {
         k_lv_move<<<sms * 8, 256, 0, c->st>>>(B);
         NB_LAUNCHED(c, "lists move");
         c->launches += 2;
-        // near-field work plan
+        // near-field work plan: leaves grouped by size class, chunk and slot offsets
         NB_TRY(nb_grow(c, c->p2p_nch, sizeof(uint32_t) * (nl + 1)));
         NB_TRY(nb_grow(c, c->p2p_work_off, sizeof(uint32_t) * (nl + 1)));
         NB_TRY(nb_grow(c, c->p2p_psize, sizeof(uint32_t) * (nl + 1)));
         NB_TRY(nb_grow(c, c->p2p_part_off, sizeof(uint32_t) * (nl + 1)));
-        k_p2p_plan<<<(unsigned)((nl + 1 + 255) / 256), 256, 0, c->st>>>(nl, DP<uint32_t>(c->leaves),
-                                                                         DP<NodeRec>(c->nodes), B.p2p_cnt,
-                                                                         DP<uint32_t>(c->p2p_nch),
-                                                                         DP<uint32_t>(c->p2p_psize));
+        NB_TRY(nb_grow(c, c->leaves_tmp, sizeof(uint32_t) * nl));
+        for (int k = 0; k < 2; ++k) {
+            NB_TRY(nb_grow(c, c->cls_key[k], sizeof(uint64_t) * nl));
+            NB_TRY(nb_grow(c, c->cls_val[k], sizeof(uint32_t) * nl));
+        }
+        // chunk / slot counts in tree order go to the offset arrays first (scratch until the scans)
+        uint32_t* nch0 = DP<uint32_t>(c->p2p_work_off);
+        uint32_t* psz0 = DP<uint32_t>(c->p2p_part_off);
+        k_p2p_plan<<<(unsigned)((nl + 255) / 256), 256, 0, c->st>>>(nl, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes),
+                                                                    B.p2p_cnt, nch0, psz0, DP<uint64_t>(c->cls_key[0]),
+                                                                    DP<uint32_t>(c->cls_val[0]));
         NB_LAUNCHED(c, "p2p plan");
-        c->launches += 1;
-        NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->p2p_nch), DP<uint32_t>(c->p2p_work_off), nl + 1,
-                           (uint32_t*)(info + INFO_P2P_WORK)));
-        NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->p2p_psize), DP<uint32_t>(c->p2p_part_off), nl + 1,
-                           (uint32_t*)(info + INFO_P2P_PART)));
+        int first = 1;
+        NB_TRY(nb_radix_sort(c, nl, DP<uint64_t>(c->cls_key[0]), DP<uint32_t>(c->cls_val[0]),
+                             DP<uint64_t>(c->cls_key[1]), DP<uint32_t>(c->cls_val[1]), 0, 3, &first));
+        const int ks = first ? 0 : 1;
+        k_p2p_order<<<(unsigned)((nl + 1 + 255) / 256), 256, 0, c->st>>>(
+            nl, DP<uint32_t>(c->leaves), DP<uint32_t>(c->leaves_tmp), nch0, psz0, DP<uint32_t>(c->p2p_nch),
+            DP<uint32_t>(c->p2p_psize), DP<uint64_t>(c->cls_key[ks]), DP<uint32_t>(c->cls_val[ks]), info);
+        NB_LAUNCHED(c, "p2p order");
+        std::swap(c->leaves, c->leaves_tmp);
+        {
+            const uint32_t* in3[3] = {DP<uint32_t>(c->p2p_nch), DP<uint32_t>(c->p2p_psize), nullptr};
+            uint32_t* out3[3] = {DP<uint32_t>(c->p2p_work_off), DP<uint32_t>(c->p2p_part_off), nullptr};
+            uint32_t* tot3[3] = {(uint32_t*)(info + INFO_P2P_WORK), (uint32_t*)(info + INFO_P2P_PART), nullptr};
+            NB_TRY(nb_scan3_u32(c, in3, out3, nl + 1, tot3));
+        }
+        k_p2p_class_work<<<1, 32, 0, c->st>>>(DP<uint32_t>(c->p2p_work_off), info);
+        NB_LAUNCHED(c, "p2p class work");
+        c->launches += 3;
         NB_CU(c, cudaMemcpyAsync(c->h_info, info, sizeof(int32_t) * INFO_WORDS, cudaMemcpyDeviceToHost, c->st));
         NB_CU(c, cudaMemcpyAsync(c->h_stats, c->stats.p, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                  c->st));

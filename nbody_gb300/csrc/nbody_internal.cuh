@@ -23,6 +23,20 @@
 #define NB_ERRBIT_ITEM_CAP 128u    // list-building work items exceeded their capacity
 
 #define NB_P2P_CHUNK 256           // partner leaves per near-field work item
+#define NB_P2P_CLASSES 6           // near-field leaf-size classes (one kernel each)
+
+// near-field class of a leaf of `count` particles: lanes per target group (CT) and targets per
+// lane (TPL) are chosen so that CT x TPL target slots fit the leaf closely
+//   class  count   CT  TPL  slots
+//     0    1-8      4   2     8
+//     1    9-16     8   2    16
+//     2    17-24    8   3    24
+//     3    25-32   16   2    32
+//     4    33-48   16   3    48
+//     5    49-     32   2    64 (larger leaves take several passes)
+__host__ __device__ __forceinline__ int nb_p2p_class(uint32_t count) {
+    return count <= 8 ? 0 : count <= 16 ? 1 : count <= 24 ? 2 : count <= 32 ? 3 : count <= 48 ? 4 : 5;
+}
 
 // layout of the small device info block (int32 words)
 enum {
@@ -45,7 +59,9 @@ enum {
     INFO_MOVED_M2L = 38,           // far-field entries moved behind the staged ones
     INFO_MOVED_P2P = 39,           // near-field entries moved behind the staged ones
     INFO_ITEMS1 = 40,              // list-building items of the current level plus one (scan length)
-    INFO_WORDS = 48
+    INFO_CLS_LEAF = 48,            // 48 .. 54: first leaf (in near-field order) of each class, then the count
+    INFO_CLS_WORK = 56,            // 56 .. 62: first near-field work item of each class, then the total
+    INFO_WORDS = 64
 };
 
 // one octree node, breadth-first order, 32 bytes
@@ -109,6 +125,7 @@ struct nbody_ctx {
     DevBuf pend_off, pend_cnt, pend_list;          // pending lists, two level parities
     DevBuf p2p_off, p2p_cnt, p2p_list, m2l_off, m2l_cnt, m2l_list;   // per-target lists
     DevBuf lst_seg, lst_nch, lst_first, lst_target, lst_cnt, lst_off, lst_cp;   // list-building work
+    DevBuf cls_key[2], cls_val[2], leaves_tmp;      // near-field class ordering of the leaves
     size_t pend_cap = 0, p2p_cap = 0, m2l_cap = 0, item_cap = 0;
     DevBuf stage;                  // host <-> device staging (interleaved doubles)
     DevBuf diag;
