@@ -161,40 +161,59 @@ __device__ __forceinline__ void adj_epilogue(const AdjP2PArgs& A, uint32_t i, co
 
 constexpr int ADJ_WARPS = 4;
 
-// One warp's share of an adjoint near-field work item: every target of the
-// leaf (two per lane, CT lanes per group) against the partner leaves
-// [s_lo, s_hi) of its list.  Per target k the pair sums are kept as
+// lanes per target group and targets per lane of the adjoint near field, per leaf-size class
+template <int CLS> struct AdjShape;
+template <> struct AdjShape<0> { static constexpr int CT = 4, TPL = 2; };
+template <> struct AdjShape<1> { static constexpr int CT = 8, TPL = 2; };
+template <> struct AdjShape<2> { static constexpr int CT = 8, TPL = 3; };
+template <> struct AdjShape<3> { static constexpr int CT = 16, TPL = 2; };
+template <> struct AdjShape<4> { static constexpr int CT = 16, TPL = 3; };
+template <> struct AdjShape<5> { static constexpr int CT = 32, TPL = 2; };
+
+// One warp's share of an adjoint near-field work item: every target of the leaf (TPL per lane, CT
+// lanes per group) against the partner leaves [s_lo, s_hi) of its list.  Per target k the pair
+// sums are kept as
 //   U = sum nu_l / s^3/2,  V = sum q_l / s^3/2,  W = sum r (r . w) / s^5/2,
 //   gq = -sum (nu_l . r) / s^3/2   (r = x_l - x_k, w = q_k nu_l - q_l nu_k)
-// and gx_k = q_k U - V nu_k - 3 W; the self pair is skipped.
-template <int MODE, bool GUARD>
-__device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE>::S4 (*tx)[P2P_TILE],
-                                         typename Prec<MODE>::S4 (*tn)[P2P_TILE], uint32_t k, const NodeRec& nt,
-                                         int64_t li, uint32_t chunk, uint32_t nchunk, uint32_t s_lo, uint32_t s_hi) {
+// and gx_k = q_k U - V nu_k - 3 W; the self pair is skipped.  Results go to the per-particle
+// buffer (single-chunk leaves) or the chunk partials; k_adj_finish adds the far-field terms.
+template <int MODE, bool GUARD, int CT, int TPL>
+__device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE>::S4* tx,
+                                         typename Prec<MODE>::S4* tn, uint32_t k, const NodeRec& nt, int64_t li,
+                                         uint32_t chunk, uint32_t nchunk, uint32_t s_lo, uint32_t s_hi) {
     typedef typename Prec<MODE>::R R;
     typedef typename Prec<MODE>::S S;
     typedef typename Prec<MODE>::S4 S4;
     constexpr bool KH = Prec<MODE>::kahan;
+    constexpr int NG = 32 / CT;
+    constexpr int TILE = P2P_WTILE / NG < 32 ? P2P_WTILE / NG : 32;
     const int lane = lane_id();
+    const int grp = lane / CT, gl = lane % CT;
+    S4* gx_t = tx + grp * TILE;
+    S4* gn_t = tn + grp * TILE;
     const double unit = A.box->unit;
     const S4* src = (const S4*)A.src;
     const S4* nu = (const S4*)A.nu;
     const uint32_t cnt_t = nt.count;
-    const int CT = cnt_t <= 16 ? 8 : cnt_t <= 32 ? 16 : 32;
-    const int NG = 32 / CT, grp = lane / CT, gl = lane % CT;
     const uint32_t loff = A.p2p_off[k];
     const S eps2 = (S)A.eps2;
     S4 zero4;
     zero4.x = 0; zero4.y = 0; zero4.z = 0; zero4.w = 0;
-    for (uint32_t tc = 0; tc < cnt_t; tc += 2 * CT) {
-        const uint32_t ta = tc + gl, tb = tc + CT + gl;
-        const bool va = ta < cnt_t, vb = tb < cnt_t;
-        const uint32_t ia = nt.begin + (va ? ta : 0), ib = nt.begin + (vb ? tb : 0);
-        const S4 ya = src[ia], yb = src[ib], na = nu[ia], nb = nu[ib];
-        // sums: U (3), V, W (3), gq per target, with compensation terms
-        S sa[8], sb_[8], ca[8], cb[8];
+    for (uint32_t tc = 0; tc < cnt_t; tc += TPL * CT) {
+        uint32_t ti[TPL], ii[TPL];
+        bool tv[TPL];
+        S4 y[TPL], nk[TPL];
+        S sum[TPL][8], cmp[TPL][8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) { sa[j] = 0; sb_[j] = 0; ca[j] = 0; cb[j] = 0; }
+        for (int j = 0; j < TPL; ++j) {
+            ti[j] = tc + gl + j * CT;
+            tv[j] = ti[j] < cnt_t;
+            ii[j] = nt.begin + (tv[j] ? ti[j] : 0);
+            y[j] = src[ii[j]];
+            nk[j] = nu[ii[j]];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) { sum[j][q] = 0; cmp[j][q] = 0; }
+        }
         for (uint32_t base = s_lo; base < s_hi; base += 32) {
             const uint32_t nbat = min(32u, s_hi - base);
             uint32_t my_s = 0, my_beg = 0, my_cnt = 0;
@@ -208,8 +227,7 @@ __device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE
                 disp(sn, nt, unit, ddx, ddy, ddz);
                 my_dx = (S)ddx; my_dy = (S)ddy; my_dz = (S)ddz;
             }
-            // partners of this batch in descending particle count: the NG groups of a round then
-            // take leaves of similar size, so fewer lanes wait on the longest one
+            // partners of this batch in descending particle count (as in the forward near field)
             {
                 const uint32_t key = (min(my_cnt, 1u << 26) << 5) | (31u - (uint32_t)lane);
                 const int from = 31 - (int)(warp_sort_desc(key) & 31u);
@@ -234,108 +252,106 @@ __device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
                 const bool self = s_id == k && q < nbat;
-                const S xa = ya.x - dx, ya_ = ya.y - dy, za = ya.z - dz;
-                const S xb = yb.x - dx, yb_ = yb.y - dy, zb = yb.z - dz;
-                for (uint32_t t0 = 0; t0 < mx; t0 += P2P_TILE) {
-                    for (int e = gl; e < P2P_TILE; e += CT) {
-                        const uint32_t j = t0 + e;
-                        tx[grp][e] = j < scnt ? src[beg + j] : zero4;
-                        tn[grp][e] = j < scnt ? nu[beg + j] : zero4;
+                S xs[TPL][3];
+#pragma unroll
+                for (int j = 0; j < TPL; ++j) { xs[j][0] = y[j].x - dx; xs[j][1] = y[j].y - dy; xs[j][2] = y[j].z - dz; }
+                for (uint32_t t0 = 0; t0 < mx; t0 += TILE) {
+                    for (int e = gl; e < TILE; e += CT) {
+                        const uint32_t jj = t0 + e;
+                        gx_t[e] = jj < scnt ? src[beg + jj] : zero4;
+                        gn_t[e] = jj < scnt ? nu[beg + jj] : zero4;
                     }
                     __syncwarp();
-                    const int nj = scnt > t0 ? min((int)(scnt - t0), P2P_TILE) : 0;
-                    const int selfa = self ? (int)ta - (int)t0 : -1, selfb = self ? (int)tb - (int)t0 : -1;
-                    S pa[8], pb[8];
+                    const int nj = scnt > t0 ? min((int)(scnt - t0), TILE) : 0;
+                    int selfe[TPL];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) { pa[j] = 0; pb[j] = 0; }
+                    for (int j = 0; j < TPL; ++j) selfe[j] = self ? (int)ti[j] - (int)t0 : -1;
+                    S p[TPL][8];
+#pragma unroll
+                    for (int j = 0; j < TPL; ++j)
+#pragma unroll
+                        for (int qq = 0; qq < 8; ++qq) p[j][qq] = 0;
 #pragma unroll 1
                     for (int e = 0; e < nj; ++e) {
-                        const S4 sx = tx[grp][e], sv = tn[grp][e];
-                        {
-                            const S rx = sx.x - xa, ry = sx.y - ya_, rz = sx.z - za;
+                        const S4 sx = gx_t[e], sv = gn_t[e];
+#pragma unroll
+                        for (int j = 0; j < TPL; ++j) {
+                            const S rx = sx.x - xs[j][0], ry = sx.y - xs[j][1], rz = sx.z - xs[j][2];
                             S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
                             if (GUARD) s2 = s2 > S(0) ? s2 : S(1e30);
                             S inv = nb_rsqrt(s2);
-                            if (e == selfa) inv = S(0);
+                            if (e == selfe[j]) inv = S(0);
                             const S inv2 = inv * inv, inv3 = inv2 * inv, inv5 = inv3 * inv2;
                             const S dl = nb_fma(sv.x, rx, nb_fma(sv.y, ry, sv.z * rz));
-                            const S dk = nb_fma(na.x, rx, nb_fma(na.y, ry, na.z * rz));
-                            const S t = nb_fma(ya.w, dl, -sx.w * dk) * inv5;
-                            pa[0] = nb_fma(sv.x, inv3, pa[0]); pa[1] = nb_fma(sv.y, inv3, pa[1]);
-                            pa[2] = nb_fma(sv.z, inv3, pa[2]); pa[3] = nb_fma(sx.w, inv3, pa[3]);
-                            pa[4] = nb_fma(rx, t, pa[4]); pa[5] = nb_fma(ry, t, pa[5]); pa[6] = nb_fma(rz, t, pa[6]);
-                            pa[7] = nb_fma(dl, inv3, pa[7]);
-                        }
-                        {
-                            const S rx = sx.x - xb, ry = sx.y - yb_, rz = sx.z - zb;
-                            S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
-                            if (GUARD) s2 = s2 > S(0) ? s2 : S(1e30);
-                            S inv = nb_rsqrt(s2);
-                            if (e == selfb) inv = S(0);
-                            const S inv2 = inv * inv, inv3 = inv2 * inv, inv5 = inv3 * inv2;
-                            const S dl = nb_fma(sv.x, rx, nb_fma(sv.y, ry, sv.z * rz));
-                            const S dk = nb_fma(nb.x, rx, nb_fma(nb.y, ry, nb.z * rz));
-                            const S t = nb_fma(yb.w, dl, -sx.w * dk) * inv5;
-                            pb[0] = nb_fma(sv.x, inv3, pb[0]); pb[1] = nb_fma(sv.y, inv3, pb[1]);
-                            pb[2] = nb_fma(sv.z, inv3, pb[2]); pb[3] = nb_fma(sx.w, inv3, pb[3]);
-                            pb[4] = nb_fma(rx, t, pb[4]); pb[5] = nb_fma(ry, t, pb[5]); pb[6] = nb_fma(rz, t, pb[6]);
-                            pb[7] = nb_fma(dl, inv3, pb[7]);
+                            const S dk = nb_fma(nk[j].x, rx, nb_fma(nk[j].y, ry, nk[j].z * rz));
+                            const S t = nb_fma(y[j].w, dl, -sx.w * dk) * inv5;
+                            p[j][0] = nb_fma(sv.x, inv3, p[j][0]); p[j][1] = nb_fma(sv.y, inv3, p[j][1]);
+                            p[j][2] = nb_fma(sv.z, inv3, p[j][2]); p[j][3] = nb_fma(sx.w, inv3, p[j][3]);
+                            p[j][4] = nb_fma(rx, t, p[j][4]); p[j][5] = nb_fma(ry, t, p[j][5]);
+                            p[j][6] = nb_fma(rz, t, p[j][6]);
+                            p[j][7] = nb_fma(dl, inv3, p[j][7]);
                         }
                     }
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        if (KH) { kahan_add(sa[j], ca[j], pa[j]); kahan_add(sb_[j], cb[j], pb[j]); }
-                        else { sa[j] += pa[j]; sb_[j] += pb[j]; }
-                    }
+                    for (int j = 0; j < TPL; ++j)
+#pragma unroll
+                        for (int qq = 0; qq < 8; ++qq) {
+                            if (KH) kahan_add(sum[j][qq], cmp[j][qq], p[j][qq]);
+                            else sum[j][qq] += p[j][qq];
+                        }
                     __syncwarp();
                 }
             }
         }
         // combine the source groups in a fixed order, in the state precision
-        R ra[8], rb[8];
+        R r[TPL][8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) { ra[j] = (R)sa[j] - (R)ca[j]; rb[j] = (R)sb_[j] - (R)cb[j]; }
+        for (int j = 0; j < TPL; ++j)
+#pragma unroll
+            for (int qq = 0; qq < 8; ++qq) r[j][qq] = (R)sum[j][qq] - (R)cmp[j][qq];
         for (int o = CT; o < 32; o <<= 1) {
 #pragma unroll
-            for (int j = 0; j < 8; ++j) { ra[j] += shfl_xor_t(ra[j], o); rb[j] += shfl_xor_t(rb[j], o); }
+            for (int j = 0; j < TPL; ++j)
+#pragma unroll
+                for (int qq = 0; qq < 8; ++qq) r[j][qq] += shfl_xor_t(r[j][qq], o);
         }
         if (grp == 0) {
-            const R qa = (R)ya.w, qb = (R)yb.w;
-            const R ga[4] = {qa * ra[0] - ra[3] * (R)na.x - R(3) * ra[4], qa * ra[1] - ra[3] * (R)na.y - R(3) * ra[5],
-                             qa * ra[2] - ra[3] * (R)na.z - R(3) * ra[6], -ra[7]};
-            const R gb[4] = {qb * rb[0] - rb[3] * (R)nb.x - R(3) * rb[4], qb * rb[1] - rb[3] * (R)nb.y - R(3) * rb[5],
-                             qb * rb[2] - rb[3] * (R)nb.z - R(3) * rb[6], -rb[7]};
             R* pt = nchunk == 1 ? (R*)A.near + 4 * (int64_t)nt.begin
                                 : (R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)chunk * cnt_t);
-            if (va) { pt[4 * ta] = ga[0]; pt[4 * ta + 1] = ga[1]; pt[4 * ta + 2] = ga[2]; pt[4 * ta + 3] = ga[3]; }
-            if (vb) { pt[4 * tb] = gb[0]; pt[4 * tb + 1] = gb[1]; pt[4 * tb + 2] = gb[2]; pt[4 * tb + 3] = gb[3]; }
+#pragma unroll
+            for (int j = 0; j < TPL; ++j) {
+                if (!tv[j]) continue;
+                const R qk = (R)y[j].w;
+                R* o = pt + 4 * ti[j];
+                o[0] = qk * r[j][0] - r[j][3] * (R)nk[j].x - R(3) * r[j][4];
+                o[1] = qk * r[j][1] - r[j][3] * (R)nk[j].y - R(3) * r[j][5];
+                o[2] = qk * r[j][2] - r[j][3] * (R)nk[j].z - R(3) * r[j][6];
+                o[3] = -r[j][7];
+            }
         }
         __syncwarp();
     }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_p2p(AdjP2PArgs A) {
+template <int MODE, int CLS>
+__global__ void __launch_bounds__(32 * ADJ_WARPS, AdjShape<CLS>::TPL == 3 ? 3 : 4)
+    k_adj_p2p(AdjP2PArgs A, int64_t li_lo, int64_t li_hi, uint32_t w_lo, uint32_t w_hi) {
     typedef typename Prec<MODE>::S4 S4;
-    __shared__ S4 tx[ADJ_WARPS][4][P2P_TILE];
-    __shared__ S4 tn[ADJ_WARPS][4][P2P_TILE];
+    constexpr int CT = AdjShape<CLS>::CT, TPL = AdjShape<CLS>::TPL;
+    __shared__ S4 tx[ADJ_WARPS][P2P_WTILE];
+    __shared__ S4 tn[ADJ_WARPS][P2P_WTILE];
     const int wib = threadIdx.x >> 5;
-    const int64_t w = (int64_t)blockIdx.x * ADJ_WARPS + wib;
-    if (w >= A.nwork) return;
-    int64_t lo = 0, hi = A.nleaves;
-    while (hi - lo > 1) {
-        const int64_t mid = (lo + hi) >> 1;
-        if (A.work_off[mid] <= (uint32_t)w) lo = mid; else hi = mid;
-    }
-    const int64_t li = lo;
-    const uint32_t chunk = (uint32_t)w - A.work_off[li];
+    const uint32_t w = w_lo + blockIdx.x * ADJ_WARPS + wib;
+    if (w >= w_hi) return;
+    const int64_t li = p2p_leaf_of(A.work_off, li_lo, li_hi, w);
+    const uint32_t chunk = w - A.work_off[li];
     const uint32_t nchunk = A.work_off[li + 1] - A.work_off[li];
     const uint32_t k = A.leaves[li];
     const NodeRec nt = A.nodes[k];
     const uint32_t lcnt = A.p2p_cnt[k];
     const uint32_t s_lo = chunk * P2P_CHUNK, s_hi = min(lcnt, s_lo + P2P_CHUNK);
-    if (A.eps2 > 0.0) adj_item<MODE, false>(A, tx[wib], tn[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
-    else adj_item<MODE, true>(A, tx[wib], tn[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
+    if (A.eps2 > 0.0) adj_item<MODE, false, CT, TPL>(A, tx[wib], tn[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
+    else adj_item<MODE, true, CT, TPL>(A, tx[wib], tn[wib], k, nt, li, chunk, nchunk, s_lo, s_hi);
 }
 
 // near-field sums of every particle (chunk partials added in chunk order), then the far-field
@@ -473,11 +489,31 @@ int force_vjp(nbody_ctx* c, double coef) {
     C.gx = c->adj_lx.p;
     C.gq = c->adj_gq.p;
     C.eps2 = c->prm.eps * c->prm.eps;
-    k_adj_p2p<MODE><<<(unsigned)((C.nwork + ADJ_WARPS - 1) / ADJ_WARPS), 32 * ADJ_WARPS, 0, c->st>>>(C);
-    NB_LAUNCHED(c, "adj_p2p");
+    {
+        const int32_t* hi = c->h_info;
+        auto one = [&](auto cls_tag) -> int {
+            constexpr int CLS = decltype(cls_tag)::value;
+            const uint32_t w0 = (uint32_t)hi[INFO_CLS_WORK + CLS], w1 = (uint32_t)hi[INFO_CLS_WORK + CLS + 1];
+            if (w1 <= w0) return NBODY_OK;
+            const int64_t l0 = (uint32_t)hi[INFO_CLS_LEAF + CLS], l1 = (uint32_t)hi[INFO_CLS_LEAF + CLS + 1];
+            k_adj_p2p<MODE, CLS><<<(w1 - w0 + ADJ_WARPS - 1) / ADJ_WARPS, 32 * ADJ_WARPS, 0, c->side[CLS]>>>(C, l0, l1,
+                                                                                                           w0, w1);
+            NB_LAUNCHED(c, "adj_p2p");
+            c->launches += 1;
+            return NBODY_OK;
+        };
+        NB_TRY(nb_fork(c));
+        NB_TRY(one(std::integral_constant<int, 5>()));
+        NB_TRY(one(std::integral_constant<int, 4>()));
+        NB_TRY(one(std::integral_constant<int, 3>()));
+        NB_TRY(one(std::integral_constant<int, 2>()));
+        NB_TRY(one(std::integral_constant<int, 1>()));
+        NB_TRY(one(std::integral_constant<int, 0>()));
+        NB_TRY(nb_join(c));
+    }
     k_adj_finish<MODE, P><<<(unsigned)((nl + ADJ_WARPS - 1) / ADJ_WARPS), 32 * ADJ_WARPS, 0, c->st>>>(C);
     NB_LAUNCHED(c, "adj_finish");
-    c->launches += 2;
+    c->launches += 1;
     if (c->timing) cudaEventRecord(c->ev[13], c->st);
     return NBODY_OK;
 }

@@ -46,6 +46,20 @@ int nb_grow(nbody_ctx* c, DevBuf& b, size_t bytes) {
     return NBODY_OK;
 }
 
+int nb_fork(nbody_ctx* c) {
+    NB_CU(c, cudaEventRecord(c->fork_ev, c->st));
+    for (int i = 0; i < NB_P2P_CLASSES; ++i) NB_CU(c, cudaStreamWaitEvent(c->side[i], c->fork_ev, 0));
+    return NBODY_OK;
+}
+
+int nb_join(nbody_ctx* c) {
+    for (int i = 0; i < NB_P2P_CLASSES; ++i) {
+        NB_CU(c, cudaEventRecord(c->join_ev[i], c->side[i]));
+        NB_CU(c, cudaStreamWaitEvent(c->st, c->join_ev[i], 0));
+    }
+    return NBODY_OK;
+}
+
 static void release(DevBuf& b) {
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
@@ -272,6 +286,11 @@ int nbody_create(const nbody_params* p, nbody_ctx** out) {
         if ((rc = nb_cuda(c, cudaMallocHost(&c->h_info, sizeof(int32_t) * INFO_WORDS), "cudaMallocHost"))) break;
         if ((rc = nb_cuda(c, cudaMemsetAsync(c->info.p, 0, sizeof(int32_t) * INFO_WORDS, c->st), "memset"))) break;
         for (int i = 0; i < 14 && !rc; ++i) rc = nb_cuda(c, cudaEventCreate(&c->ev[i]), "cudaEventCreate");
+        for (int i = 0; i < NB_P2P_CLASSES && !rc; ++i) {
+            rc = nb_cuda(c, cudaStreamCreateWithFlags(&c->side[i], cudaStreamNonBlocking), "cudaStreamCreate");
+            if (!rc) rc = nb_cuda(c, cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming), "cudaEventCreate");
+        }
+        if (!rc) rc = nb_cuda(c, cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming), "cudaEventCreate");
     } while (0);
     if (rc) {
         g_create_err = c->err;
@@ -304,6 +323,11 @@ int nbody_destroy(nbody_ctx* c) {
     if (c->h_info) cudaFreeHost(c->h_info);
     for (int i = 0; i < 16; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    for (int i = 0; i < NB_P2P_CLASSES; ++i) {
+        if (c->side[i]) cudaStreamSynchronize(c->side[i]), cudaStreamDestroy(c->side[i]);
+        if (c->join_ev[i]) cudaEventDestroy(c->join_ev[i]);
+    }
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
     return NBODY_OK;

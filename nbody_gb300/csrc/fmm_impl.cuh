@@ -767,18 +767,21 @@ int p2p_launch_classes(nbody_ctx* c, const P2PArgs& B) {
         const uint32_t w0 = (uint32_t)hi[INFO_CLS_WORK + CLS], w1 = (uint32_t)hi[INFO_CLS_WORK + CLS + 1];
         if (w1 <= w0) return NBODY_OK;
         const int64_t l0 = (uint32_t)hi[INFO_CLS_LEAF + CLS], l1 = (uint32_t)hi[INFO_CLS_LEAF + CLS + 1];
-        k_p2p<MODE, P, POT, CLS><<<(w1 - w0 + P2P_WARPS - 1) / P2P_WARPS, 32 * P2P_WARPS, 0, c->st>>>(B, l0, l1, w0, w1);
+        k_p2p<MODE, P, POT, CLS><<<(w1 - w0 + P2P_WARPS - 1) / P2P_WARPS, 32 * P2P_WARPS, 0, c->side[CLS]>>>(B, l0, l1,
+                                                                                                      w0, w1);
         NB_LAUNCHED(c, "p2p");
         c->launches += 1;
         return NBODY_OK;
     };
+    // the classes write disjoint particles: run them side by side so no launch tail idles the GPU
+    NB_TRY(nb_fork(c));
     NB_TRY(one(std::integral_constant<int, 5>()));
     NB_TRY(one(std::integral_constant<int, 4>()));
     NB_TRY(one(std::integral_constant<int, 3>()));
     NB_TRY(one(std::integral_constant<int, 2>()));
     NB_TRY(one(std::integral_constant<int, 1>()));
     NB_TRY(one(std::integral_constant<int, 0>()));
-    return NBODY_OK;
+    return nb_join(c);
 }
 template <int MODE, int P>
 int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {

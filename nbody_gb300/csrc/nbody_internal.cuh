@@ -101,6 +101,8 @@ struct nbody_ctx {
     nbody_params prm;
     int device = 0;
     cudaStream_t st = nullptr;
+    cudaStream_t side[NB_P2P_CLASSES] = {};   // near-field class kernels run side by side
+    cudaEvent_t fork_ev = nullptr, join_ev[NB_P2P_CLASSES] = {};
     int64_t n = 0;
     double time = 0.0;
     bool have_acc = false;
@@ -193,6 +195,11 @@ int nb_build_tree(nbody_ctx* c);
 
 // interaction lists and near-field work plan of the current tree (lists.cu); syncs once
 int nb_build_lists(nbody_ctx* c);
+
+// side streams: nb_fork makes them wait for the main stream's work so far, nb_join makes the main
+// stream wait for what was queued on them since (api.cu)
+int nb_fork(nbody_ctx* c);
+int nb_join(nbody_ctx* c);
 
 // one force evaluation at the current positions (api.cu); kdk = 1 applies the opening kick and drift first
 int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot);
