@@ -203,7 +203,8 @@ int nbody_get_interactions(nbody_ctx* c, int which, int64_t* npairs, int32_t* pa
    keys, 1 sort + gather, 2 tree, 3 upward pass (P2M, M2M), 4 interaction
    lists, 5 far field (M2L, L2L), 6 near field + L2P + integration; and of the
    last nbody_force_vjp: 7 adjoint seeds + L2P transpose, 8 L2L transpose,
-   9 M2L transpose, 10 M2M transpose, 11 near field + P2M/L2P adjoints.
+   9 M2L transpose, 10 M2M transpose (the near field runs alongside 7-10 on
+   side streams), 11 the rest of the near field + the P2M/L2P adjoints.
    n <= 12.  Timing is enabled by nbody_set_timing(c, 1). */
 int nbody_set_timing(nbody_ctx* c, int on);
 int nbody_phase_times(nbody_ctx* c, float* ms, int n);

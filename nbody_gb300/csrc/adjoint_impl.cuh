@@ -426,6 +426,48 @@ int force_vjp(nbody_ctx* c, double coef) {
     k_adj_prep<MODE><<<(unsigned)((n + 255) / 256), 256, 0, c->st>>>(A);
     NB_LAUNCHED(c, "adj_prep");
     c->launches += 1;
+    // near field on the side streams (it needs only the seeds), far-field chain meanwhile on the main one
+    AdjP2PArgs C;
+    C.leaves = DP<uint32_t>(c->leaves);
+    C.nleaves = nl;
+    C.nodes = DP<NodeRec>(c->nodes);
+    C.box = box;
+    C.src = c->src.p;
+    C.nu = c->adj_nu.p;
+    C.L = c->L.p;
+    C.lamM = c->adj_lamM.p;
+    C.p2p_off = DP<uint32_t>(c->p2p_off); C.p2p_cnt = DP<uint32_t>(c->p2p_cnt); C.p2p_list = DP<uint32_t>(c->p2p_list);
+    C.work_off = DP<uint32_t>(c->p2p_work_off);
+    C.nwork = (uint32_t)c->h_info[INFO_P2P_WORK];
+    C.part_off = DP<uint32_t>(c->p2p_part_off);
+    C.part = c->p2p_part.p;
+    NB_TRY(nb_grow(c, c->adj_near, 4 * sizeof(R) * (size_t)n));
+    C.near = c->adj_near.p;
+    C.ids = DP<uint32_t>(c->id[cur]);
+    C.gx = c->adj_lx.p;
+    C.gq = c->adj_gq.p;
+    C.eps2 = c->prm.eps * c->prm.eps;
+    {
+        const int32_t* hi = c->h_info;
+        auto one = [&](auto cls_tag) -> int {
+            constexpr int CLS = decltype(cls_tag)::value;
+            const uint32_t w0 = (uint32_t)hi[INFO_CLS_WORK + CLS], w1 = (uint32_t)hi[INFO_CLS_WORK + CLS + 1];
+            if (w1 <= w0) return NBODY_OK;
+            const int64_t l0 = (uint32_t)hi[INFO_CLS_LEAF + CLS], l1 = (uint32_t)hi[INFO_CLS_LEAF + CLS + 1];
+            k_adj_p2p<MODE, CLS><<<(w1 - w0 + ADJ_WARPS - 1) / ADJ_WARPS, 32 * ADJ_WARPS, 0, c->side[CLS]>>>(C, l0, l1,
+                                                                                                           w0, w1);
+            NB_LAUNCHED(c, "adj_p2p");
+            c->launches += 1;
+            return NBODY_OK;
+        };
+        NB_TRY(nb_fork(c));
+        NB_TRY(one(std::integral_constant<int, 5>()));
+        NB_TRY(one(std::integral_constant<int, 4>()));
+        NB_TRY(one(std::integral_constant<int, 3>()));
+        NB_TRY(one(std::integral_constant<int, 2>()));
+        NB_TRY(one(std::integral_constant<int, 1>()));
+        NB_TRY(one(std::integral_constant<int, 0>()));
+    }
     k_adj_l2pT<MODE, P><<<(unsigned)((nl + 3) / 4), 128, 0, c->st>>>(
         nl, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes), DP<S4>(c->src), DP<S4>(c->adj_nu), DP<H>(c->adj_lamL),
         lamL32);
@@ -469,48 +511,7 @@ int force_vjp(nbody_ctx* c, double coef) {
         c->launches += 1;
     }
     if (c->timing) cudaEventRecord(c->ev[12], c->st);
-    AdjP2PArgs C;
-    C.leaves = DP<uint32_t>(c->leaves);
-    C.nleaves = nl;
-    C.nodes = DP<NodeRec>(c->nodes);
-    C.box = box;
-    C.src = c->src.p;
-    C.nu = c->adj_nu.p;
-    C.L = c->L.p;
-    C.lamM = c->adj_lamM.p;
-    C.p2p_off = DP<uint32_t>(c->p2p_off); C.p2p_cnt = DP<uint32_t>(c->p2p_cnt); C.p2p_list = DP<uint32_t>(c->p2p_list);
-    C.work_off = DP<uint32_t>(c->p2p_work_off);
-    C.nwork = (uint32_t)c->h_info[INFO_P2P_WORK];
-    C.part_off = DP<uint32_t>(c->p2p_part_off);
-    C.part = c->p2p_part.p;
-    NB_TRY(nb_grow(c, c->adj_near, 4 * sizeof(R) * (size_t)n));
-    C.near = c->adj_near.p;
-    C.ids = DP<uint32_t>(c->id[cur]);
-    C.gx = c->adj_lx.p;
-    C.gq = c->adj_gq.p;
-    C.eps2 = c->prm.eps * c->prm.eps;
-    {
-        const int32_t* hi = c->h_info;
-        auto one = [&](auto cls_tag) -> int {
-            constexpr int CLS = decltype(cls_tag)::value;
-            const uint32_t w0 = (uint32_t)hi[INFO_CLS_WORK + CLS], w1 = (uint32_t)hi[INFO_CLS_WORK + CLS + 1];
-            if (w1 <= w0) return NBODY_OK;
-            const int64_t l0 = (uint32_t)hi[INFO_CLS_LEAF + CLS], l1 = (uint32_t)hi[INFO_CLS_LEAF + CLS + 1];
-            k_adj_p2p<MODE, CLS><<<(w1 - w0 + ADJ_WARPS - 1) / ADJ_WARPS, 32 * ADJ_WARPS, 0, c->side[CLS]>>>(C, l0, l1,
-                                                                                                           w0, w1);
-            NB_LAUNCHED(c, "adj_p2p");
-            c->launches += 1;
-            return NBODY_OK;
-        };
-        NB_TRY(nb_fork(c));
-        NB_TRY(one(std::integral_constant<int, 5>()));
-        NB_TRY(one(std::integral_constant<int, 4>()));
-        NB_TRY(one(std::integral_constant<int, 3>()));
-        NB_TRY(one(std::integral_constant<int, 2>()));
-        NB_TRY(one(std::integral_constant<int, 1>()));
-        NB_TRY(one(std::integral_constant<int, 0>()));
-        NB_TRY(nb_join(c));
-    }
+    NB_TRY(nb_join(c));
     k_adj_finish<MODE, P><<<(unsigned)((nl + ADJ_WARPS - 1) / ADJ_WARPS), 32 * ADJ_WARPS, 0, c->st>>>(C);
     NB_LAUNCHED(c, "adj_finish");
     c->launches += 1;

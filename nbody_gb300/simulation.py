@@ -237,7 +237,7 @@ class CudaSimulation:
         check(self._h, _lib.load().nbody_set_timing(self._h, int(on)))
 
     PHASES = ("kick_drift_keys", "sort_gather", "tree", "upward", "lists", "far_field", "near_field")
-    VJP_PHASES = ("adj_seed_l2pT", "adj_l2lT", "adj_m2lT", "adj_m2mT", "adj_near")
+    VJP_PHASES = ("adj_seed_l2pT", "adj_l2lT", "adj_m2lT", "adj_m2mT", "adj_near_rest_finish")
 
     def phase_times(self):
         """Device ms of the last force evaluation's phases (PHASES)."""
