@@ -330,8 +330,9 @@ __global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A)
         fence_mbar_init();
     }
     __syncwarp();
-    // issue the bulk copies of batch b into stage b & 1; returns this lane's source
-    auto issue = [&](uint32_t b) -> uint32_t {
+    // issue the bulk copies of batch b into stage b & 1; returns this lane's source node record
+    // (loaded now, used one batch later, so its latency hides behind the current batch)
+    auto issue = [&](uint32_t b) -> NodeRec {
         const uint32_t nb = min(32u, cnt - 32 * b);
         const uint32_t k = b & 1;
         const uint32_t s = (uint32_t)lane < nb ? A.m2l_list[off + 32 * b + lane] : 0u;
@@ -340,19 +341,19 @@ __global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A)
         if (lane == 0) mbar_expect_tx(&bar[k], nb * ROWB);
         __syncwarp();
         if ((uint32_t)lane < nb) bulk_g2s(rows + (k * 32 + lane) * SST, Msrc + (int64_t)s * TM, ROWB, &bar[k]);
-        return s;
+        return A.nodes[s];
     };
     bool failed = false;
     uint32_t b_fail = 0;
-    uint32_t s_next = nbatch ? issue(0) : 0u;
+    NodeRec sn_next;
+    if (nbatch) sn_next = issue(0);
     for (uint32_t b = 0; b < nbatch; ++b) {
-        const uint32_t s_cur = s_next;
+        const NodeRec sn = sn_next;
         const uint32_t k = b & 1;
         const uint32_t nb = min(32u, cnt - 32 * b);
-        if (b + 1 < nbatch) s_next = issue(b + 1);
+        if (b + 1 < nbatch) sn_next = issue(b + 1);
         if (!mbar_wait_warp(&bar[k], (b >> 1) & 1)) { failed = true; b_fail = b; break; }
         if ((uint32_t)lane < nb) {
-            const NodeRec sn = A.nodes[s_cur];
             int sx, sy, sz;
             centre_fine32(sn, sx, sy, sz);
             const S dx = (S)(tcx - sx) * unit, dy = (S)(tcy - sy) * unit, dz = (S)(tcz - sz) * unit;
