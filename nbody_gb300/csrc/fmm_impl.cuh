@@ -376,7 +376,11 @@ __global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A)
         if (b_fail + 1 < nbatch) mbar_wait_warp(&bar[(b_fail + 1) & 1], ((b_fail + 1) >> 1) & 1);
         return;
     }
-    H* Lg = (H*)A.L;
+    // lane-order butterfly sums; lane a % 32 keeps coefficient a and converts only its own
+    constexpr int NPL = (T + 31) / 32;
+    S own[NPL];
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) own[j] = S(0);
 #pragma unroll
     for (int a = 0; a < T; ++a) {
         S v;
@@ -384,8 +388,12 @@ __global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A)
         else v = Lreg[a];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += shfl_xor_t(v, o);
-        if ((a & 31) == lane) Lg[t * T + a] = (H)v;
+        if ((a & 31) == lane) own[a >> 5] = v;
     }
+    H* Lg = (H*)A.L;
+#pragma unroll
+    for (int j = 0; j < NPL; ++j)
+        if (lane + 32 * j < T) Lg[t * T + lane + 32 * j] = (H)own[j];
 }
 
 // ---------------------------------------------------------------------------
