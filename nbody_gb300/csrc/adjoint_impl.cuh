@@ -223,9 +223,7 @@ __device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE
                 const NodeRec sn = A.nodes[my_s];
                 my_beg = sn.begin;
                 my_cnt = sn.count;
-                double ddx, ddy, ddz;
-                disp(sn, nt, unit, ddx, ddy, ddz);
-                my_dx = (S)ddx; my_dy = (S)ddy; my_dz = (S)ddz;
+                disp_s<S>(sn, nt, unit, my_dx, my_dy, my_dz);
             }
             // partners of this batch in descending particle count (as in the forward near field)
             {
@@ -303,18 +301,12 @@ __device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE
                 }
             }
         }
-        // combine the source groups in a fixed order, in the state precision
+        // combine the source groups in a fixed order
         R r[TPL][8];
 #pragma unroll
         for (int j = 0; j < TPL; ++j)
 #pragma unroll
-            for (int qq = 0; qq < 8; ++qq) r[j][qq] = (R)sum[j][qq] - (R)cmp[j][qq];
-        for (int o = CT; o < 32; o <<= 1) {
-#pragma unroll
-            for (int j = 0; j < TPL; ++j)
-#pragma unroll
-                for (int qq = 0; qq < 8; ++qq) r[j][qq] += shfl_xor_t(r[j][qq], o);
-        }
+            for (int qq = 0; qq < 8; ++qq) r[j][qq] = group_sum<MODE>(sum[j][qq], cmp[j][qq], CT);
         if (grp == 0) {
             R* pt = nchunk == 1 ? (R*)A.near + 4 * (int64_t)nt.begin
                                 : (R*)A.part + 4 * ((int64_t)A.part_off[li] + (int64_t)chunk * cnt_t);

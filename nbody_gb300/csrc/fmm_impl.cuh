@@ -78,6 +78,43 @@ __device__ __forceinline__ T shfl_xor_t(T v, int o) {
     return __shfl_xor_sync(0xffffffffu, v, o);
 }
 
+// centre displacement (a - b) in the bulk precision: the fine-unit difference is an integer below
+// 2^23 and the fine unit a power of two, so the FP32 product equals the rounded FP64 one exactly
+template <typename S>
+__device__ __forceinline__ void disp_s(const NodeRec& a, const NodeRec& b, double unit, S& dx, S& dy, S& dz) {
+    int ax, ay, az, bx, by, bz;
+    centre_fine32(a, ax, ay, az);
+    centre_fine32(b, bx, by, bz);
+    const S u = (S)unit;
+    dx = (S)(ax - bx) * u;
+    dy = (S)(ay - by) * u;
+    dz = (S)(az - bz) * u;
+}
+
+// Sum of a compensated pair (value = hi - comp) over the lane groups o = CT .. 16 of a butterfly,
+// returned in the state precision.  Mixed form: the pairs are added in FP32 with an error-free
+// two-sum, converted to FP64 once; otherwise the sum runs in R.
+template <int MODE>
+__device__ __forceinline__ typename Prec<MODE>::R group_sum(typename Prec<MODE>::S hi, typename Prec<MODE>::S comp,
+                                                            int CT) {
+    typedef typename Prec<MODE>::R R;
+    if constexpr (Prec<MODE>::kahan) {
+        float h = hi, l = -comp;
+        for (int o = CT; o < 32; o <<= 1) {
+            const float h2 = __shfl_xor_sync(0xffffffffu, h, o), l2 = __shfl_xor_sync(0xffffffffu, l, o);
+            const float sum = h + h2, bb = sum - h;
+            const float e = (h - (sum - bb)) + (h2 - bb);
+            h = sum;
+            l = l + l2 + e;
+        }
+        return (R)h + (R)l;
+    } else {
+        R v = (R)hi - (R)comp;
+        for (int o = CT; o < 32; o <<= 1) v += shfl_xor_t(v, o);
+        return v;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // P2M at leaves + particle offsets
 // ---------------------------------------------------------------------------
@@ -578,9 +615,7 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
                 const NodeRec sn = A.nodes[my_s];
                 my_beg = sn.begin;
                 my_cnt = sn.count;
-                double ddx, ddy, ddz;
-                disp(sn, nt, unit, ddx, ddy, ddz);
-                my_dx = (S)ddx; my_dy = (S)ddy; my_dz = (S)ddz;
+                disp_s<S>(sn, nt, unit, my_dx, my_dy, my_dz);
             }
             // partners of this batch in descending particle count: the NG groups of a round then
             // take leaves of similar size, so fewer lanes wait on the longest one
@@ -672,18 +707,12 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
                 sb = nsb;
             }
         }
-        // combine the source groups in a fixed order, in the state precision
+        // combine the source groups in a fixed order
         R tot[TPL][4];
 #pragma unroll
         for (int j = 0; j < TPL; ++j)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) tot[j][q] = (R)acc[j][q] - (R)cmp[j][q];
-        for (int o = CT; o < 32; o <<= 1) {
-#pragma unroll
-            for (int j = 0; j < TPL; ++j)
-#pragma unroll
-                for (int q = 0; q < (POT ? 4 : 3); ++q) tot[j][q] += shfl_xor_t(tot[j][q], o);
-        }
+            for (int q = 0; q < 4; ++q) tot[j][q] = (POT || q < 3) ? group_sum<MODE>(acc[j][q], cmp[j][q], CT) : R(0);
         if (grp == 0) {
 #pragma unroll
             for (int j = 0; j < TPL; ++j) {
