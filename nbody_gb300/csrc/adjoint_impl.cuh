@@ -277,7 +277,7 @@ __device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE
                             const S rx = sx.x - xs[j][0], ry = sx.y - xs[j][1], rz = sx.z - xs[j][2];
                             S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
                             if (GUARD) s2 = s2 > S(0) ? s2 : S(1e30);
-                            S inv = nb_rsqrt(s2);
+                            S inv = GUARD ? nb_rsqrt(s2) : nb_rsqrt_n(s2);
                             if (e == selfe[j]) inv = S(0);
                             const S inv2 = inv * inv, inv3 = inv2 * inv, inv5 = inv3 * inv2;
                             const S dl = nb_fma(sv.x, rx, nb_fma(sv.y, ry, sv.z * rz));

@@ -686,7 +686,7 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
                         const S rx = sj.x - xs[j][0], ry = sj.y - xs[j][1], rz = sj.z - xs[j][2];
                         S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
                         if (GUARD) s2 = s2 > S(0) ? s2 : S(1e30);
-                        S inv = nb_rsqrt(s2);
+                        S inv = GUARD ? nb_rsqrt(s2) : nb_rsqrt_n(s2);
                         if (self && sb + e == ti[j]) inv = S(0);
                         const S w = sj.w * inv * inv * inv;
                         p[j][0] = nb_fma(rx, w, p[j][0]);

@@ -61,7 +61,7 @@ def gen_derivs(p, o):
     o.append("  template <int ST = 1>")
     o.append(f"  static __device__ __forceinline__ void derivs(S x, S y, S z, S eps2, S* D) {{")
     o.append("    const S s = x * x + y * y + z * z + eps2;")
-    o.append("    D[0] = nb_rsqrt(s);")
+    o.append("    D[0] = nb_rsqrt_n(s);")
     o.append("    const S is = D[0] * D[0];")
     X = ["x", "y", "z"]
     for n in terms(p)[1:]:

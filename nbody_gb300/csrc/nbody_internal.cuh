@@ -233,6 +233,14 @@ __device__ __forceinline__ void nb_ld4(const double* p, double* o) {
     o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
 }
 __device__ __forceinline__ double nb_rsqrt(double s) { return rsqrt(s); }
+// rsqrt for arguments known to be normal (bounded below by a softening or a cell separation): the
+// PTX approximation with flush-to-zero, one special-function instruction, no subnormal handling
+__device__ __forceinline__ float nb_rsqrt_n(float s) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
+    return r;
+}
+__device__ __forceinline__ double nb_rsqrt_n(double s) { return rsqrt(s); }
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ uint32_t lanemask_lt() { return (1u << lane_id()) - 1u; }
