@@ -145,6 +145,45 @@ public:
         return acc;
     }
 
+    /* FP64 diagnostics of the current state (nbody_diagnostics: kinetic and potential energy,
+       momentum, angular momentum, mass) */
+    std::vector<double> diagnostics() {
+        std::vector<double> out(9);
+        check(nbody_diagnostics(_ctx, out.data()), "nbody_diagnostics");
+        return out;
+    }
+
+    /* adjoint of one force evaluation: for S = sum_i mu_i . a_i (mu n x 3, input order) fills
+       dS/dx (n x 3), dS/dq and dS/dm (n) */
+    void forceVjp(std::vector<double> const& mu, std::vector<double>& gx, std::vector<double>& gq,
+                  std::vector<double>& gm) {
+        gx.assign(3 * _n, 0.0);
+        gq.assign(_n, 0.0);
+        gm.assign(_n, 0.0);
+        check(nbody_force_vjp(_ctx, mu.data(), gx.data(), gq.data(), gm.data()), "nbody_force_vjp");
+    }
+
+    /* nsteps leapfrog steps recorded for backward(): snapshots every `every` steps, or every
+       evaluation kept whole with every = 0; returns the time after the last step */
+    Scalar forwardCheckpointed(int nsteps, int every) {
+        double t = 0.0;
+        check(nbody_forward_checkpointed(_ctx, nsteps, every, &t), "nbody_forward_checkpointed");
+        return (Scalar)t;
+    }
+
+    /* reverse sweep of the recorded run: from dL/dx_N and dL/dv_N (n x 3, input order; empty =
+       zero) to dL/dx_0, dL/dv_0 (n x 3), dL/dq and dL/dm (n) */
+    void backward(std::vector<double> const& gxT, std::vector<double> const& gvT, std::vector<double>& gx0,
+                  std::vector<double>& gv0, std::vector<double>& gq, std::vector<double>& gm) {
+        gx0.assign(3 * _n, 0.0);
+        gv0.assign(3 * _n, 0.0);
+        gq.assign(_n, 0.0);
+        gm.assign(_n, 0.0);
+        check(nbody_backward(_ctx, gxT.empty() ? nullptr : gxT.data(), gvT.empty() ? nullptr : gvT.data(),
+                             gx0.data(), gv0.data(), gq.data(), gm.data()),
+              "nbody_backward");
+    }
+
     nbody_ctx* handle() const { return _ctx; }
 };
 

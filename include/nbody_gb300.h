@@ -213,6 +213,10 @@ int nbody_phase_times(nbody_ctx* c, float* ms, int n);
    own work after the step. */
 void* nbody_stream(nbody_ctx* c);
 
+/* Device memory held by the context (its grow-only work buffers, snapshots and
+   records) and its high-water mark since nbody_create, in bytes. */
+int nbody_device_memory(nbody_ctx* c, int64_t* current, int64_t* peak);
+
 /* Simulated time. */
 int nbody_get_time(nbody_ctx* c, double* t);
 

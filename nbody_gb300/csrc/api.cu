@@ -29,6 +29,7 @@ int nb_grow(nbody_ctx* c, DevBuf& b, size_t bytes) {
     if (b.p) {
         NB_CU(c, cudaStreamSynchronize(c->st));
         NB_CU(c, cudaFree(b.p));
+        c->dev_bytes -= b.bytes;
         b.p = nullptr;
         b.bytes = 0;
     }
@@ -43,6 +44,8 @@ int nb_grow(nbody_ctx* c, DevBuf& b, size_t bytes) {
     NB_TRY(nb_cuda(c, e, "cudaMalloc"));
     b.p = p;
     b.bytes = want;
+    c->dev_bytes += want;
+    c->dev_peak = std::max(c->dev_peak, c->dev_bytes);
     return NBODY_OK;
 }
 
@@ -534,6 +537,13 @@ int nbody_phase_times(nbody_ctx* c, float* ms, int n) {
 }
 
 void* nbody_stream(nbody_ctx* c) { return c ? (void*)c->st : nullptr; }
+
+int nbody_device_memory(nbody_ctx* c, int64_t* current, int64_t* peak) {
+    if (!c) return NBODY_ERR_INVALID;
+    if (current) *current = (int64_t)c->dev_bytes;
+    if (peak) *peak = (int64_t)c->dev_peak;
+    return NBODY_OK;
+}
 
 int nbody_get_time(nbody_ctx* c, double* t) {
     if (!c || !t) return NBODY_ERR_INVALID;

@@ -135,6 +135,7 @@ struct nbody_ctx {
     DevBuf p2p_nch, p2p_work_off, p2p_psize, p2p_part_off, p2p_part;   // near-field work plan
     unsigned long long h_stats[8] = {0};
     int64_t launches = 0;          // kernels launched by the last force evaluation
+    size_t dev_bytes = 0, dev_peak = 0;   // device memory held by the context, and its high-water mark
 
     // small device blocks + pinned mirrors
     DevBuf info, box, bbox;

@@ -227,6 +227,12 @@ class CudaSimulation:
                                                   ptr(gm)))
         return gx0, gv0, gq, gm
 
+    def device_memory(self):
+        """(bytes held on the device now, high-water mark since creation)."""
+        cur, peak = C.c_int64(), C.c_int64()
+        check(self._h, _lib.load().nbody_device_memory(self._h, C.byref(cur), C.byref(peak)))
+        return cur.value, peak.value
+
     def stats(self):
         out = np.zeros(7, np.int64)
         check(self._h, _lib.load().nbody_get_stats(self._h, ptr(out), 7))

@@ -42,3 +42,37 @@ def test_cpp_drop_in_matches_python_binding(nb, tmp_path):
     assert count == n
     assert abs(t_cpp - np.float32(t)) == 0
     assert abs(checksum - ref) <= 1e-12 * abs(ref)
+
+
+def test_cpp_adjoint_matches_python_binding(nb, tmp_path):
+    """Recorded run + reverse sweep through the C++ class equals the Python binding's, bitwise."""
+    cxx = shutil.which("g++")
+    assert cxx, "g++ is needed to build the C++ adjoint test"
+    from nbody_gb300 import _lib, ics
+    exe = tmp_path / "adjoint"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    subprocess.run([cxx, "-std=c++14", "-O2", "-ffp-contract=off", "-Wall", "-Wextra", "-pedantic", "-I",
+                    os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "adjoint_main.cpp"), "-L", libdir, "-lnbody_gb300",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    pos, vel, m = ics.plummer(3000, seed=78)
+    data = np.zeros((len(m), 8), np.float32)
+    data[:, :3], data[:, 3:6], data[:, 6], data[:, 7] = pos, vel, m, m
+    f = tmp_path / "particles.f32"
+    data.tofile(f)
+    out = subprocess.run([str(exe), str(len(m)), "4", "2", str(f)], check=True, capture_output=True,
+                         text=True).stdout.split()
+    got = [float(out[i]) for i in (1, 3, 5, 7)]
+    d = data.astype(np.float64)
+    sim = nb.CudaSimulation.from_arrays(d[:, :3], d[:, 3:6], d[:, 6], d[:, 7], precision=nb.PREC_FP64, order=6,
+                                        leaf_capacity=16, fixed_box=0, eps=0.01, dt=np.float32(1e-3),
+                                        integrator=nb.INTEG_LEAPFROG)
+    sim.forward_checkpointed(4, 2)
+    xT = sim.state("input")[0].astype(np.float32).astype(np.float64)
+    gx0, gv0, gq, gm = sim.backward(xT, None)
+    # the C++ checksums are sequential sums (particle-major, then x, y, z; no fused multiply-adds):
+    # sum the same way
+    w = np.array([1.0, 2.0, 3.0])
+    seq = lambda a: float(np.cumsum(a.ravel())[-1])
+    want = [seq(gx0 * w), seq(gv0 * w), seq(gq), seq(gm)]
+    for g, e in zip(got, want):
+        assert abs(g - e) <= 1e-14 * max(abs(e), 1e-300)
