@@ -319,7 +319,7 @@ int nbody_destroy(nbody_ctx* c) {
                       &c->m2l_list, &c->stage, &c->diag, &c->info, &c->box, &c->bbox, &c->adj_lx, &c->adj_lv,
                       &c->adj_gq, &c->adj_gm, &c->adj_nu, &c->adj_lamL, &c->adj_lamL32, &c->adj_lamM, &c->adj_near,
                       &c->snaps, &c->lst_seg, &c->lst_nch, &c->lst_first, &c->lst_target, &c->lst_cnt,
-                      &c->lst_off, &c->lst_cp, &c->cls_key[0], &c->cls_key[1], &c->cls_val[0], &c->cls_val[1],
+                      &c->lst_off, &c->lst_cp, &c->lst_rows, &c->cls_key[0], &c->cls_key[1], &c->cls_val[0], &c->cls_val[1],
                       &c->leaves_tmp})
         release(*b);
     for (EvalRecord& r : c->recs) release(r.buf);

@@ -14,12 +14,12 @@
 //                           level r+1; t a leaf: refined by t itself at r+1).
 // Work is split into items (target, chunk of 32 input partners) so a target
 // with a long input list (a large sparse leaf next to a dense region) is
-// spread over many warps.  Each level runs a count pass and a write pass with
-// exclusive scans in between, so every target's output of the level is one
-// contiguous block in a fixed order; a final pass concatenates each target's
-// blocks in level order into the per-target lists the far- and near-field
-// kernels read.  Nothing depends on scheduling: the lists are bitwise
-// reproducible.
+// spread over many warps.  Each level classifies every candidate once into a
+// per-item staging row, scans the per-item counts, and scatters the rows, so
+// every target's output of the level is one contiguous block in a fixed order;
+// a final pass concatenates each target's blocks in level order into the
+// per-target lists the far- and near-field kernels read.  Nothing depends on
+// scheduling: the lists are bitwise reproducible.
 #include <algorithm>
 
 #include "nbody_internal.cuh"
@@ -44,6 +44,7 @@ struct LevelArgs {
     uint32_t *m2l_stage, *p2p_stage;
     uint32_t m2l_cap, p2p_cap;
     uint32_t *m2l_soff, *m2l_scnt, *p2p_soff, *p2p_scnt;   // rows of level r
+    uint32_t* rows;                                   // per item: its classified candidates (CANDS each)
     int32_t* info;
     unsigned long long* stats;
 };
@@ -103,9 +104,10 @@ __global__ void k_lv_fill(LevelArgs A) {
     for (uint32_t c = 0; c < n; ++c) A.target[f + c] = (uint32_t)t;
 }
 
-// Classifies the candidates of item i; WRITE = false counts, true writes.
-template <bool WRITE>
-__device__ void lv_item(const LevelArgs& A, uint32_t i, uint32_t* cand) {
+// Classifies the candidates of item i once: each goes to row i of the staging table (candidate
+// order, class in the top two bits: 1 far field, 2 near field, 3 pending) and the item's three
+// counts are kept for the scans; k_lv_scatter then places the row's entries.
+__device__ void lv_classify(const LevelArgs& A, uint32_t i, uint32_t* cand) {
     const int lane = lane_id();
     const uint32_t t = A.target[i];
     const NodeRec nt = A.nodes[t];
@@ -128,21 +130,7 @@ __device__ void lv_item(const LevelArgs& A, uint32_t i, uint32_t* cand) {
     const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
     for (uint32_t u = 0; u < ns; ++u) cand[inc - ns + u] = cb + u;
     __syncwarp();
-    // output positions of this item (write pass)
-    uint32_t o_m = 0, o_p = 0, o_q = 0;
-    bool ok_m = true, ok_p = true, ok_q = true;
-    if (WRITE) {
-        const uint32_t bm = (uint32_t)A.info[INFO_BASE_M2L], bp = (uint32_t)A.info[INFO_BASE_P2P];
-        o_m = bm + A.off[0][i];
-        o_p = bp + A.off[1][i];
-        o_q = A.off[2][i];
-        ok_m = (uint64_t)o_m + A.cnt[0][i] <= A.m2l_cap;
-        ok_p = (uint64_t)o_p + A.cnt[1][i] <= A.p2p_cap;
-        ok_q = (uint64_t)o_q + A.cnt[2][i] <= A.pend_cap;
-        if (lane == 0 && !(ok_m && ok_p && ok_q))
-            atomicOr((unsigned int*)&A.info[INFO_ERR],
-                     (ok_m ? 0u : NB_ERRBIT_M2L_CAP) | (ok_p ? 0u : NB_ERRBIT_P2P_CAP) | (ok_q ? 0u : NB_ERRBIT_PEND_CAP));
-    }
+    uint32_t* row = A.rows + (size_t)i * CANDS;
     uint32_t nm = 0, np = 0, nq = 0;
     unsigned long long near_particles = 0;
     for (uint32_t g = 0; g < total; g += 32) {
@@ -156,46 +144,24 @@ __device__ void lv_item(const LevelArgs& A, uint32_t i, uint32_t* cand) {
         const bool sleaf = valid && sn.nchild == 0;
         const bool near = valid && !approx && tleaf && sleaf;
         const bool pend = valid && !approx && !near;
-        const uint32_t mm = __ballot_sync(0xffffffffu, approx);
-        const uint32_t mp = __ballot_sync(0xffffffffu, near);
-        const uint32_t mq = __ballot_sync(0xffffffffu, pend);
-        if (WRITE) {
-            const uint32_t lt = lanemask_lt();
-            if (approx && ok_m) A.m2l_stage[o_m + nm + __popc(mm & lt)] = sc;
-            if (near && ok_p) A.p2p_stage[o_p + np + __popc(mp & lt)] = sc;
-            if (pend && ok_q) A.pout_list[o_q + nq + __popc(mq & lt)] = sc;
-            if (near) near_particles += sn.count;
-        }
-        nm += __popc(mm);
-        np += __popc(mp);
-        nq += __popc(mq);
-    }
-    if (!WRITE) {
-        if (lane == 0) { A.cnt[0][i] = nm; A.cnt[1][i] = np; A.cnt[2][i] = nq; }
-        return;
+        if (valid) row[g + lane] = sc | ((approx ? 1u : near ? 2u : 3u) << 30);
+        if (near) near_particles += sn.count;
+        nm += __popc(__ballot_sync(0xffffffffu, approx));
+        np += __popc(__ballot_sync(0xffffffffu, near));
+        nq += __popc(__ballot_sync(0xffffffffu, pend));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) near_particles += __shfl_xor_sync(0xffffffffu, near_particles, o);
     if (lane == 0) {
+        A.cnt[0][i] = nm; A.cnt[1][i] = np; A.cnt[2][i] = nq;
         if (near_particles) atomicAdd(&A.stats[1], near_particles * nt.count);
-        if (chunk == 0) {
-            // the target's blocks of this level: its first item's offset, through the end of its last
-            const uint32_t e = i + A.nch[t];
-            A.m2l_soff[t] = o_m;
-            A.m2l_scnt[t] = A.off[0][e] - A.off[0][i];
-            A.p2p_soff[t] = o_p;
-            A.p2p_scnt[t] = A.off[1][e] - A.off[1][i];
-            A.pout_off[t] = o_q;
-            A.pout_cnt[t] = A.off[2][e] - A.off[2][i];
-        }
     }
 }
 
-template <bool WRITE>
-__global__ void __launch_bounds__(32 * LW) k_lv_items(LevelArgs A) {
+__global__ void __launch_bounds__(32 * LW) k_lv_classify(LevelArgs A) {
     __shared__ uint32_t s_cand[LW][CANDS];
     const uint32_t items = (uint32_t)A.info[INFO_ITEMS];
-    if (!WRITE && blockIdx.x == 0 && threadIdx.x == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         // the scans cover items + 1 entries: the last one (zero) gives every target's end
         const uint32_t m = items < A.item_cap ? items : A.item_cap;
         A.cnt[0][m] = 0; A.cnt[1][m] = 0; A.cnt[2][m] = 0;
@@ -204,8 +170,56 @@ __global__ void __launch_bounds__(32 * LW) k_lv_items(LevelArgs A) {
     if (items > A.item_cap || lists_failed(A.info)) return;
     const uint32_t stride = gridDim.x * LW;
     for (uint32_t i = blockIdx.x * LW + (threadIdx.x >> 5); i < items; i += stride) {
-        lv_item<WRITE>(A, i, s_cand[threadIdx.x >> 5]);
+        lv_classify(A, i, s_cand[threadIdx.x >> 5]);
         __syncwarp();
+    }
+}
+
+// Places the staged entries of every item at its scanned offsets (candidate order within each
+// class); the first item of a target records the target's blocks of this level.
+__global__ void __launch_bounds__(32 * LW) k_lv_scatter(LevelArgs A) {
+    const uint32_t items = (uint32_t)A.info[INFO_ITEMS];
+    if (items > A.item_cap || lists_failed(A.info)) return;
+    const int lane = lane_id();
+    const uint32_t bm = (uint32_t)A.info[INFO_BASE_M2L], bp = (uint32_t)A.info[INFO_BASE_P2P];
+    const uint32_t stride = gridDim.x * LW;
+    for (uint32_t i = blockIdx.x * LW + (threadIdx.x >> 5); i < items; i += stride) {
+        const uint32_t o_m = bm + A.off[0][i], o_p = bp + A.off[1][i], o_q = A.off[2][i];
+        const uint32_t c_m = A.cnt[0][i], c_p = A.cnt[1][i], c_q = A.cnt[2][i];
+        const bool ok_m = (uint64_t)o_m + c_m <= A.m2l_cap, ok_p = (uint64_t)o_p + c_p <= A.p2p_cap,
+                   ok_q = (uint64_t)o_q + c_q <= A.pend_cap;
+        if (lane == 0 && !(ok_m && ok_p && ok_q))
+            atomicOr((unsigned int*)&A.info[INFO_ERR],
+                     (ok_m ? 0u : NB_ERRBIT_M2L_CAP) | (ok_p ? 0u : NB_ERRBIT_P2P_CAP) | (ok_q ? 0u : NB_ERRBIT_PEND_CAP));
+        const uint32_t total = c_m + c_p + c_q;
+        const uint32_t* row = A.rows + (size_t)i * CANDS;
+        const uint32_t lt = lanemask_lt();
+        uint32_t nm = 0, np = 0, nq = 0;
+        for (uint32_t g = 0; g < total; g += 32) {
+            const uint32_t e = g + lane < total ? row[g + lane] : 0u;
+            const uint32_t cl = e >> 30, sc = e & 0x3fffffffu;
+            const uint32_t mm = __ballot_sync(0xffffffffu, cl == 1), mp = __ballot_sync(0xffffffffu, cl == 2),
+                           mq = __ballot_sync(0xffffffffu, cl == 3);
+            if (cl == 1 && ok_m) A.m2l_stage[o_m + nm + __popc(mm & lt)] = sc;
+            if (cl == 2 && ok_p) A.p2p_stage[o_p + np + __popc(mp & lt)] = sc;
+            if (cl == 3 && ok_q) A.pout_list[o_q + nq + __popc(mq & lt)] = sc;
+            nm += __popc(mm);
+            np += __popc(mp);
+            nq += __popc(mq);
+        }
+        if (lane == 0) {
+            const uint32_t t = A.target[i];
+            if (i == A.first[t]) {
+                // the target's blocks of this level: its first item's offset, through the end of its last
+                const uint32_t e = i + A.nch[t];
+                A.m2l_soff[t] = o_m;
+                A.m2l_scnt[t] = A.off[0][e] - A.off[0][i];
+                A.p2p_soff[t] = o_p;
+                A.p2p_scnt[t] = A.off[1][e] - A.off[1][i];
+                A.pout_off[t] = o_q;
+                A.pout_cnt[t] = A.off[2][e] - A.off[2][i];
+            }
+        }
     }
 }
 
@@ -389,6 +403,7 @@ int nb_build_lists(nbody_ctx* c) {
         NB_TRY(nb_grow(c, c->p2p_list, sizeof(uint32_t) * c->p2p_cap));
         NB_TRY(nb_grow(c, c->m2l_list, sizeof(uint32_t) * c->m2l_cap));
         NB_TRY(nb_grow(c, c->lst_target, sizeof(uint32_t) * c->item_cap));
+        NB_TRY(nb_grow(c, c->lst_rows, sizeof(uint32_t) * CANDS * c->item_cap));
         NB_TRY(nb_grow(c, c->lst_cnt, sizeof(uint32_t) * 3 * (c->item_cap + 1)));
         NB_TRY(nb_grow(c, c->lst_off, sizeof(uint32_t) * 3 * (c->item_cap + 1)));
         NB_CU(c, cudaMemsetAsync(c->stats.p, 0, 8 * sizeof(unsigned long long), c->st));
@@ -414,6 +429,7 @@ int nb_build_lists(nbody_ctx* c) {
         A.first = DP<uint32_t>(c->lst_first);
         A.target = DP<uint32_t>(c->lst_target);
         A.item_cap = (uint32_t)c->item_cap;
+        A.rows = DP<uint32_t>(c->lst_rows);
         for (int k = 0; k < 3; ++k) { A.cnt[k] = cnt + k * ic; A.off[k] = off + k * ic; }
         A.m2l_stage = DP<uint32_t>(c->m2l_list);
         A.p2p_stage = DP<uint32_t>(c->p2p_list);
@@ -436,8 +452,8 @@ int nb_build_lists(nbody_ctx* c) {
             NB_LAUNCHED(c, "lists plan");
             NB_TRY(nb_scan_u32(c, A.nch, A.first, A.hi + 1, (uint32_t*)(info + INFO_ITEMS)));
             k_lv_fill<<<gt, 256, 0, c->st>>>(A);
-            k_lv_items<false><<<sms * 8, 32 * LW, 0, c->st>>>(A);
-            NB_LAUNCHED(c, "lists count");
+            k_lv_classify<<<sms * 8, 32 * LW, 0, c->st>>>(A);
+            NB_LAUNCHED(c, "lists classify");
             // per-item offsets; one extra entry past the last item gives each target's end
             {
                 const uint32_t* in3[3] = {A.cnt[0], A.cnt[1], A.cnt[2]};
@@ -446,8 +462,8 @@ int nb_build_lists(nbody_ctx* c) {
                                      (uint32_t*)(info + INFO_LVL_PEND)};
                 NB_TRY(nb_scan3_u32(c, in3, out3, (int64_t)c->item_cap + 1, tot3, (const uint32_t*)(info + INFO_ITEMS1)));
             }
-            k_lv_items<true><<<sms * 8, 32 * LW, 0, c->st>>>(A);
-            NB_LAUNCHED(c, "lists write");
+            k_lv_scatter<<<sms * 8, 32 * LW, 0, c->st>>>(A);
+            NB_LAUNCHED(c, "lists scatter");
             c->launches += 4;
         }
         // per-target lists: blocks left in place, multi-block targets concatenated in level order

@@ -126,7 +126,7 @@ struct nbody_ctx {
     DevBuf M, M32, L, src;
     DevBuf pend_off, pend_cnt, pend_list;          // pending lists, two level parities
     DevBuf p2p_off, p2p_cnt, p2p_list, m2l_off, m2l_cnt, m2l_list;   // per-target lists
-    DevBuf lst_seg, lst_nch, lst_first, lst_target, lst_cnt, lst_off, lst_cp;   // list-building work
+    DevBuf lst_seg, lst_nch, lst_first, lst_target, lst_cnt, lst_off, lst_cp, lst_rows;   // list-building work
     DevBuf cls_key[2], cls_val[2], leaves_tmp;      // near-field class ordering of the leaves
     size_t pend_cap = 0, p2p_cap = 0, m2l_cap = 0, item_cap = 0;
     DevBuf stage;                  // host <-> device staging (interleaved doubles)
