@@ -141,7 +141,7 @@ int rec_fields(nbody_ctx* c, int64_t nn, int64_t nl, uint32_t m2l_ext, uint32_t 
     const int p = c->prm.order;
     const size_t terms = (size_t)(p + 1) * (p + 2) * (p + 3) / 6;
     const size_t s4 = c->prm.precision == NBODY_PREC_FP64 ? 32 : 16;
-    const size_t hs = c->prm.precision == NBODY_PREC_FP32 ? 4 : 8;
+    const size_t hs = c->prm.precision == NBODY_PREC_FP64 ? 8 : 4;
     int i = 0;
     f[i++] = {&c->nodes, sizeof(NodeRec) * (size_t)nn};
     f[i++] = {&c->leaves, sizeof(uint32_t) * (size_t)nl};

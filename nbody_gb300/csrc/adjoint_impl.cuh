@@ -401,9 +401,8 @@ int force_vjp(nbody_ctx* c, double coef) {
     const BoxDev* box = DP<BoxDev>(c->box);
     NB_TRY(nb_grow(c, c->adj_nu, sizeof(S4) * n));
     NB_TRY(nb_grow(c, c->adj_lamL, sizeof(H) * TM * nn));
-    if (MODE == NBODY_PREC_MIXED) NB_TRY(nb_grow(c, c->adj_lamL32, sizeof(float) * TM * nn));
     NB_TRY(nb_grow(c, c->adj_lamM, sizeof(H) * T * nn));
-    float* lamL32 = MODE == NBODY_PREC_MIXED ? DP<float>(c->adj_lamL32) : nullptr;
+    float* lamL32 = nullptr;   // the transposed M2L reads lamL directly
 
     AdjArgs A;
     A.n = n;
@@ -479,7 +478,7 @@ int force_vjp(nbody_ctx* c, double coef) {
         M2LArgs B;
         B.nodes = DP<NodeRec>(c->nodes);
         B.box = box;
-        B.Mm2l = MODE == NBODY_PREC_MIXED ? (const void*)lamL32 : (const void*)c->adj_lamL.p;
+        B.Mm2l = c->adj_lamL.p;
         B.L = c->adj_lamM.p;
         B.m2l_off = DP<uint32_t>(c->m2l_off); B.m2l_cnt = DP<uint32_t>(c->m2l_cnt);
         B.m2l_list = DP<uint32_t>(c->m2l_list);

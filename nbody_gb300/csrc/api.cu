@@ -314,10 +314,10 @@ int nbody_destroy(nbody_ctx* c) {
             release(*b);
     for (DevBuf* b : {&c->pot, &c->stats, &c->p2p_nch, &c->p2p_work_off, &c->p2p_psize, &c->p2p_part_off,
                       &c->p2p_part, &c->hist, &c->hist_scan, &c->scan_part, &c->cpl, &c->wnd, &c->leaflvl, &c->nc, &c->pfx,
-                      &c->nodes, &c->leafflag, &c->leafpfx, &c->leaves, &c->M, &c->M32, &c->L, &c->src, &c->pend_off,
+                      &c->nodes, &c->leafflag, &c->leafpfx, &c->leaves, &c->M, &c->L, &c->src, &c->pend_off,
                       &c->pend_cnt, &c->p2p_off, &c->p2p_cnt, &c->pend_list, &c->p2p_list, &c->m2l_off, &c->m2l_cnt,
                       &c->m2l_list, &c->stage, &c->diag, &c->info, &c->box, &c->bbox, &c->adj_lx, &c->adj_lv,
-                      &c->adj_gq, &c->adj_gm, &c->adj_nu, &c->adj_lamL, &c->adj_lamL32, &c->adj_lamM, &c->adj_near,
+                      &c->adj_gq, &c->adj_gm, &c->adj_nu, &c->adj_lamL, &c->adj_lamM, &c->adj_near,
                       &c->snaps, &c->lst_seg, &c->lst_nch, &c->lst_first, &c->lst_target, &c->lst_cnt,
                       &c->lst_off, &c->lst_cp, &c->lst_rows, &c->cls_key[0], &c->cls_key[1], &c->cls_val[0], &c->cls_val[1],
                       &c->leaves_tmp})

@@ -44,7 +44,7 @@ template <> struct Prec<NBODY_PREC_FP32> {
 template <> struct Prec<NBODY_PREC_MIXED> {
     typedef double R;
     typedef float S;
-    typedef double H;
+    typedef float H;   // FP32 shifts of offsets formed from the FP64 cell centres (the FP64 pipe is 1/64 rate)
     typedef float4 S4;
     static constexpr bool kahan = true;
     static constexpr bool lane_smem = false;
@@ -832,10 +832,9 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     const int cur = c->cur;
     constexpr int TM = nb_tm<P>::value;
     NB_TRY(nb_grow(c, c->M, sizeof(H) * TM * nn));
-    if (MODE == NBODY_PREC_MIXED) NB_TRY(nb_grow(c, c->M32, sizeof(float) * TM * nn));
     NB_TRY(nb_grow(c, c->L, sizeof(H) * T * nn));
     NB_TRY(nb_grow(c, c->src, sizeof(S4) * n));
-    float* M32 = MODE == NBODY_PREC_MIXED ? DP<float>(c->M32) : nullptr;
+    float* M32 = nullptr;   // M2L reads the stored multipoles directly (they are in the bulk precision)
     const BoxDev* box = DP<BoxDev>(c->box);
 
     if (c->timing) cudaEventRecord(c->ev[3], c->st);
@@ -860,7 +859,7 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
         M2LArgs B;
         B.nodes = DP<NodeRec>(c->nodes);
         B.box = box;
-        B.Mm2l = MODE == NBODY_PREC_MIXED ? (const void*)M32 : (const void*)c->M.p;
+        B.Mm2l = c->M.p;
         B.L = c->L.p;
         B.m2l_off = DP<uint32_t>(c->m2l_off); B.m2l_cnt = DP<uint32_t>(c->m2l_cnt);
         B.m2l_list = DP<uint32_t>(c->m2l_list);

@@ -123,7 +123,7 @@ struct nbody_ctx {
     int level_start[NB_LEVELS + 3] = {0};
 
     // expansions and lists
-    DevBuf M, M32, L, src;
+    DevBuf M, L, src;
     DevBuf pend_off, pend_cnt, pend_list;          // pending lists, two level parities
     DevBuf p2p_off, p2p_cnt, p2p_list, m2l_off, m2l_cnt, m2l_list;   // per-target lists
     DevBuf lst_seg, lst_nch, lst_first, lst_target, lst_cnt, lst_off, lst_cp, lst_rows;   // list-building work
@@ -143,7 +143,7 @@ struct nbody_ctx {
     double* h_box = nullptr;
 
     // adjoint (input-order accumulators, adjoint expansions, trajectory snapshots)
-    DevBuf adj_lx, adj_lv, adj_gq, adj_gm, adj_nu, adj_lamL, adj_lamL32, adj_lamM, adj_near;
+    DevBuf adj_lx, adj_lv, adj_gq, adj_gm, adj_nu, adj_lamL, adj_lamM, adj_near;
     DevBuf snaps;                  // sorted-state snapshots: checkpoints, segment scratch, final state
     size_t snap_bytes = 0;         // bytes of one snapshot
     int ck_steps = 0;              // steps of the recorded run (0: nothing recorded)
