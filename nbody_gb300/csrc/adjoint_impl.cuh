@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(128) k_adj_l2pT(int64_t nleaves, const uint32_
                                                   const NodeRec* __restrict__ nodes,
                                                   const typename Prec<MODE>::S4* __restrict__ src,
                                                   const typename Prec<MODE>::S4* __restrict__ nu,
-                                                  typename Prec<MODE>::H* __restrict__ lamL, float* __restrict__ lamL32) {
+                                                  typename Prec<MODE>::H* __restrict__ lamL) {
     typedef typename Prec<MODE>::S S;
     typedef typename Prec<MODE>::H H;
     constexpr int T = nb_terms<P>::value;
@@ -111,7 +111,6 @@ __global__ void __launch_bounds__(128) k_adj_l2pT(int64_t nleaves, const uint32_
         if (a < T) {
             const H v = (H)acc[j] * (H)nb_invfact[a];
             lamL[(int64_t)k * TM + a] = v;
-            if (lamL32) lamL32[(int64_t)k * TM + a] = (float)v;
         }
     }
 }
@@ -402,7 +401,6 @@ int force_vjp(nbody_ctx* c, double coef) {
     NB_TRY(nb_grow(c, c->adj_nu, sizeof(S4) * n));
     NB_TRY(nb_grow(c, c->adj_lamL, sizeof(H) * TM * nn));
     NB_TRY(nb_grow(c, c->adj_lamM, sizeof(H) * T * nn));
-    float* lamL32 = nullptr;   // the transposed M2L reads lamL directly
 
     AdjArgs A;
     A.n = n;
@@ -460,8 +458,7 @@ int force_vjp(nbody_ctx* c, double coef) {
         NB_TRY(one(std::integral_constant<int, 0>()));
     }
     k_adj_l2pT<MODE, P><<<(unsigned)((nl + 3) / 4), 128, 0, c->st>>>(
-        nl, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes), DP<S4>(c->src), DP<S4>(c->adj_nu), DP<H>(c->adj_lamL),
-        lamL32);
+        nl, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes), DP<S4>(c->src), DP<S4>(c->adj_nu), DP<H>(c->adj_lamL));
     NB_LAUNCHED(c, "adj_l2pT");
     c->launches += 1;
     if (c->timing) cudaEventRecord(c->ev[9], c->st);
@@ -469,7 +466,7 @@ int force_vjp(nbody_ctx* c, double coef) {
         const int lo = c->level_start[l], hi = c->level_start[l + 1];
         if (hi <= lo) continue;
         k_m2m<MODE, P><<<(unsigned)((hi - lo + 3) / 4), 128, 0, c->st>>>(lo, hi, DP<NodeRec>(c->nodes), box,
-                                                                         DP<H>(c->adj_lamL), lamL32);
+                                                                         DP<H>(c->adj_lamL));
         NB_LAUNCHED(c, "adj_l2lT");
         c->launches += 1;
     }

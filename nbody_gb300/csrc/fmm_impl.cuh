@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(128) k_p2m(int64_t nleaves, const uint32_t* __
                                              const typename Prec<MODE>::R* __restrict__ z,
                                              const typename Prec<MODE>::R* __restrict__ q,
                                              typename Prec<MODE>::S4* __restrict__ src,
-                                             typename Prec<MODE>::H* __restrict__ M, float* __restrict__ M32) {
+                                             typename Prec<MODE>::H* __restrict__ M) {
     typedef typename Prec<MODE>::R R;
     typedef typename Prec<MODE>::S S;
     typedef typename Prec<MODE>::H H;
@@ -187,7 +187,6 @@ __global__ void __launch_bounds__(128) k_p2m(int64_t nleaves, const uint32_t* __
         if (a < T) {
             H v = (H)acc[j] * (H)nb_invfact[a];
             M[(int64_t)k * TM + a] = v;
-            if (M32) M32[(int64_t)k * TM + a] = (float)v;
         }
     }
 }
@@ -197,8 +196,7 @@ __global__ void __launch_bounds__(128) k_p2m(int64_t nleaves, const uint32_t* __
 // ---------------------------------------------------------------------------
 template <int MODE, int P>
 __global__ void __launch_bounds__(128) k_m2m(int lo, int hi, const NodeRec* __restrict__ nodes,
-                                             const BoxDev* __restrict__ boxp, typename Prec<MODE>::H* __restrict__ M,
-                                             float* __restrict__ M32) {
+                                             const BoxDev* __restrict__ boxp, typename Prec<MODE>::H* __restrict__ M) {
     typedef typename Prec<MODE>::H H;
     constexpr int T = nb_terms<P>::value;
     constexpr int TM = nb_tm<P>::value;
@@ -248,7 +246,6 @@ __global__ void __launch_bounds__(128) k_m2m(int lo, int hi, const NodeRec* __re
         int a = lane + 32 * j;
         if (a < T) {
             M[(int64_t)k * TM + a] = acc[j];
-            if (M32) M32[(int64_t)k * TM + a] = (float)acc[j];
         }
     }
 }
@@ -834,20 +831,19 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     NB_TRY(nb_grow(c, c->M, sizeof(H) * TM * nn));
     NB_TRY(nb_grow(c, c->L, sizeof(H) * T * nn));
     NB_TRY(nb_grow(c, c->src, sizeof(S4) * n));
-    float* M32 = nullptr;   // M2L reads the stored multipoles directly (they are in the bulk precision)
     const BoxDev* box = DP<BoxDev>(c->box);
 
     if (c->timing) cudaEventRecord(c->ev[3], c->st);
     k_p2m<MODE, P><<<(unsigned)((c->nleaves + 3) / 4), 128, 0, c->st>>>(
         c->nleaves, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes), box, DP<R>(c->x[cur]), DP<R>(c->y[cur]),
-        DP<R>(c->z[cur]), DP<R>(c->q[cur]), DP<S4>(c->src), DP<H>(c->M), M32);
+        DP<R>(c->z[cur]), DP<R>(c->q[cur]), DP<S4>(c->src), DP<H>(c->M));
     NB_LAUNCHED(c, "p2m");
     c->launches += 1;
     for (int l = c->depth - 1; l >= 0; --l) {
         const int lo = c->level_start[l], hi = c->level_start[l + 1];
         if (hi <= lo) continue;
         k_m2m<MODE, P><<<(unsigned)((hi - lo + 3) / 4), 128, 0, c->st>>>(lo, hi, DP<NodeRec>(c->nodes), box,
-                                                                         DP<H>(c->M), M32);
+                                                                         DP<H>(c->M));
         NB_LAUNCHED(c, "m2m");
         c->launches += 1;
     }
