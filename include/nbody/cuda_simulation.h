@@ -184,6 +184,13 @@ public:
               "nbody_backward");
     }
 
+    /* trajectory file in the row format of the reference's particles.csv, one row every `every`
+       steps (order 0: leaf order as particles(), 1: input order) */
+    void writeTrajectory(const char* path, int every = 1, int order = 0, int digits = 6) {
+        check(nbody_trajectory_open(_ctx, path, every, order, digits), "nbody_trajectory_open");
+    }
+    void closeTrajectory() { check(nbody_trajectory_close(_ctx), "nbody_trajectory_close"); }
+
     nbody_ctx* handle() const { return _ctx; }
 };
 

@@ -136,6 +136,19 @@ int nbody_forward_checkpointed(nbody_ctx* c, int nsteps, int every, double* t_ou
 int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* gx0, double* gv0, double* gq,
                    double* gm);
 
+/* Trajectory file (replaces the CSV dump of src/main.cpp:77-101, same row
+   format: the time, then x,y,z of every particle, comma separated, one row per
+   written step).  After nbody_trajectory_open, every `every`-th step taken by
+   nbody_step appends a row; order = 0 writes particles in the current leaf
+   order (what the reference's particles() returns), order = 1 in input order;
+   digits = significant digits (the reference's stream default is 6).
+   Positions are copied asynchronously and formatted by a writer thread; a
+   step waits only when three rows are still being written.
+   nbody_trajectory_close (also done by nbody_set_state and nbody_destroy)
+   flushes and closes the file and reports a failed write. */
+int nbody_trajectory_open(nbody_ctx* c, const char* path, int every, int order, int digits);
+int nbody_trajectory_close(nbody_ctx* c);
+
 /* FP64 diagnostics of the current state: out[0] kinetic energy, out[1]
    potential energy, out[2..4] momentum, out[5..7] angular momentum,
    out[8] total mass.  (The reference computes none.) */

@@ -26,7 +26,7 @@ EXPORTS = ("nbody_default_params", "nbody_create", "nbody_destroy", "nbody_set_s
            "nbody_get_interactions", "nbody_set_timing", "nbody_phase_times", "nbody_stream", "nbody_get_time",
            "nbody_last_error", "nbody_direct_forces", "nbody_get_stats", "nbody_flops_per_m2l", "nbody_flops_per_p2p",
            "nbody_measure_peaks", "nbody_direct_forces_static", "nbody_force_vjp", "nbody_forward_checkpointed",
-           "nbody_backward", "nbody_device_memory")
+           "nbody_backward", "nbody_device_memory", "nbody_trajectory_open", "nbody_trajectory_close")
 
 
 class Params(C.Structure):
@@ -77,6 +77,8 @@ def load(path: str | None = None):
     L.nbody_forward_checkpointed.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.nbody_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.nbody_device_memory.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.nbody_trajectory_open.argtypes = [vp, C.c_char_p, C.c_int, C.c_int, C.c_int]
+    L.nbody_trajectory_close.argtypes = [vp]
     L.nbody_compute_forces.argtypes = [vp, vp, vp]
     L.nbody_diagnostics.argtypes = [vp, vp]
     L.nbody_tree_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),

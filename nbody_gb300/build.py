@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnbody_gb300.so")
-UNITS = ["api.cu", "sort.cu", "tree.cu", "direct.cu", "direct_static.cu", "fmm_fp32.cu", "fmm_mixed.cu", "fmm_fp64.cu", "adjoint.cu", "lists.cu"]
+UNITS = ["api.cu", "sort.cu", "tree.cu", "direct.cu", "direct_static.cu", "fmm_fp32.cu", "fmm_mixed.cu", "fmm_fp64.cu", "adjoint.cu", "lists.cu", "trajectory.cu"]
 HEADERS = ["nbody_internal.cuh", "fmm_impl.cuh", "adjoint_impl.cuh", "fmm_ops.inc", "../../include/nbody_gb300.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",

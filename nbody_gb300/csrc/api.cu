@@ -308,6 +308,7 @@ int nbody_destroy(nbody_ctx* c) {
     if (!c) return NBODY_OK;
     cudaSetDevice(c->device);
     if (c->st) cudaStreamSynchronize(c->st);
+    nb_traj_close(c);
     for (int k = 0; k < 2; ++k)
         for (DevBuf* b : {&c->x[k], &c->y[k], &c->z[k], &c->vx[k], &c->vy[k], &c->vz[k], &c->ax[k], &c->ay[k], &c->az[k],
                           &c->m[k], &c->q[k], &c->id[k], &c->keys[k], &c->vals[k], &c->seedk[k], &c->seedv[k]})
@@ -342,6 +343,7 @@ int nbody_set_state(nbody_ctx* c, int64_t n, const double* pos, const double* ve
     if (n < 1 || n > (int64_t)0x7fffffff) return nb_fail(c, NBODY_ERR_INVALID, "n must be in 1..2^31-1");
     if (!pos || !mass) return nb_fail(c, NBODY_ERR_INVALID, "pos and mass are required");
     NB_CU(c, cudaSetDevice(c->device));
+    NB_TRY(nb_traj_close(c));   // a trajectory file holds one particle set
     c->n = n;
     c->cur = 0;
     NB_TRY(alloc_state(c, n));
@@ -414,6 +416,7 @@ int nbody_step(nbody_ctx* c, int nsteps, double* t_out) {
             c->have_acc = false;
         }
         c->time += c->prm.dt;
+        NB_TRY(nb_traj_capture(c));
     }
     NB_CU(c, cudaStreamSynchronize(c->st));
     if (t_out) *t_out = c->time;

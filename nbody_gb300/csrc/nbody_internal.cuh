@@ -97,6 +97,8 @@ struct EvalRecord {
     int32_t info[INFO_WORDS] = {0};
 };
 
+struct nb_traj;   // trajectory writer (trajectory.cu)
+
 struct nbody_ctx {
     nbody_params prm;
     int device = 0;
@@ -159,6 +161,8 @@ struct nbody_ctx {
     cudaEvent_t ev[16] = {};       // 0..7 force evaluation, 8..13 force VJP
     float phase_ms[16] = {0};
 
+    nb_traj* traj = nullptr;       // open trajectory file, if any
+
     std::string err;
 };
 
@@ -201,6 +205,10 @@ int nb_build_lists(nbody_ctx* c);
 // stream wait for what was queued on them since (api.cu)
 int nb_fork(nbody_ctx* c);
 int nb_join(nbody_ctx* c);
+
+// trajectory rows after a step, and closing the writer (trajectory.cu)
+int nb_traj_capture(nbody_ctx* c);
+int nb_traj_close(nbody_ctx* c);
 
 // one force evaluation at the current positions (api.cu); kdk = 1 applies the opening kick and drift first
 int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot);

@@ -227,6 +227,15 @@ class CudaSimulation:
                                                   ptr(gm)))
         return gx0, gv0, gq, gm
 
+    def trajectory_open(self, path, every: int = 1, order: str = "leaf", digits: int = 6):
+        """Append a CSV row (time, x, y, z of every particle) every `every` steps, as the reference's
+        main loop writes particles.csv; order 'leaf' (the reference's) or 'input'."""
+        check(self._h, _lib.load().nbody_trajectory_open(self._h, str(path).encode(), int(every),
+                                                         1 if order == "input" else 0, int(digits)))
+
+    def trajectory_close(self):
+        check(self._h, _lib.load().nbody_trajectory_close(self._h))
+
     def device_memory(self):
         """(bytes held on the device now, high-water mark since creation)."""
         cur, peak = C.c_int64(), C.c_int64()

@@ -60,16 +60,18 @@ def test_c1_precision_study(nb):
     pos, vel, m = ics.workload("cube256k", seed=52)
     tg = np.random.default_rng(52).choice(len(m), 8192, replace=False)
     err = {}
-    ref = None
+    ref = {}
     for prec in ("fp32", "mixed", "fp64"):
         p = {"fp32": nb.PREC_FP32, "mixed": nb.PREC_MIXED, "fp64": nb.PREC_FP64}[prec]
         for theta in (0.3, 0.5, 0.7):
             sim = nb.CudaSimulation.from_arrays(pos, vel, m, m, precision=p, order=5, leaf_capacity=32, fixed_box=0,
                                                 theta=theta, eps=1e-3)
             acc = sim.forces()
-            if ref is None:
-                ref, _ = sim.direct(tg)
-            err[prec, theta] = _rms_rel(acc[tg], ref)
+            # the FP32 form holds FP32-rounded positions: its direct sum is taken at those
+            key = prec == "fp32"
+            if key not in ref:
+                ref[key], _ = sim.direct(tg)
+            err[prec, theta] = _rms_rel(acc[tg], ref[key])
             sim.close()
     for prec in ("mixed", "fp64"):
         assert err[prec, 0.3] < err[prec, 0.5] < err[prec, 0.7], err

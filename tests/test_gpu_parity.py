@@ -221,3 +221,25 @@ def test_errors_are_reported(nb):
         s = nb.CudaSimulation.from_arrays(np.array([[np.nan, 0, 0], [0, 0, 0]]), None, np.ones(2), fixed_box=0,
                                           precision=nb.PREC_MIXED)
         s.forces()
+
+
+def test_trajectory_file_rows(nb, tmp_path):
+    """Rows every 2 steps, the reference's particles.csv format, in input and in leaf order."""
+    pos, vel, m = ics.plummer(1500, seed=38)
+    for order in ("input", "leaf"):
+        sim = nb.CudaSimulation.from_arrays(pos, vel, m, m, precision=nb.PREC_MIXED, order=4, leaf_capacity=16,
+                                            fixed_box=0, dt=1e-3, integrator=nb.INTEG_LEAPFROG)
+        f = tmp_path / f"traj_{order}.csv"
+        sim.trajectory_open(f, every=2, order=order, digits=17)
+        want = []
+        for _ in range(3):
+            t = sim.step(2)
+            want.append((t, sim.state(order)[0]))
+        sim.step(1)                       # an odd step writes no row
+        sim.trajectory_close()
+        rows = [np.array(line.split(","), dtype=np.float64) for line in f.read_text().splitlines()]
+        assert len(rows) == 3
+        for row, (t, p) in zip(rows, want):
+            assert row[0] == t
+            np.testing.assert_array_equal(row[1:].reshape(-1, 3), p)
+        sim.close()
