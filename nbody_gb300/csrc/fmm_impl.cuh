@@ -364,12 +364,16 @@ __global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A)
         fence_mbar_init();
     }
     __syncwarp();
-    // issue the bulk copies of batch b into stage b & 1; returns this lane's source node record
-    // (loaded now, used one batch later, so its latency hides behind the current batch)
-    auto issue = [&](uint32_t b) -> NodeRec {
+    // this lane's list entry of batch b (0 past the end)
+    auto entry = [&](uint32_t b) -> uint32_t {
+        const uint32_t j = 32 * b + lane;
+        return b < nbatch && j < cnt ? A.m2l_list[off + j] : 0u;
+    };
+    // issue the bulk copies of batch b (source s of this lane, loaded one batch earlier) into stage
+    // b & 1; returns the lane's source node record, loaded now and used one batch later
+    auto issue = [&](uint32_t b, uint32_t s) -> NodeRec {
         const uint32_t nb = min(32u, cnt - 32 * b);
         const uint32_t k = b & 1;
-        const uint32_t s = (uint32_t)lane < nb ? A.m2l_list[off + 32 * b + lane] : 0u;
         fence_proxy_async();
         __syncwarp();
         if (lane == 0) mbar_expect_tx(&bar[k], nb * ROWB);
@@ -380,12 +384,16 @@ __global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A)
     bool failed = false;
     uint32_t b_fail = 0;
     NodeRec sn_next;
-    if (nbatch) sn_next = issue(0);
+    uint32_t s_ahead = entry(1);       // list entries run two batches ahead of the computation
+    if (nbatch) sn_next = issue(0, entry(0));
     for (uint32_t b = 0; b < nbatch; ++b) {
         const NodeRec sn = sn_next;
         const uint32_t k = b & 1;
         const uint32_t nb = min(32u, cnt - 32 * b);
-        if (b + 1 < nbatch) sn_next = issue(b + 1);
+        if (b + 1 < nbatch) {
+            sn_next = issue(b + 1, s_ahead);
+            s_ahead = entry(b + 2);
+        }
         if (!mbar_wait_warp(&bar[k], (b >> 1) & 1)) { failed = true; b_fail = b; break; }
         if ((uint32_t)lane < nb) {
             int sx, sy, sz;
