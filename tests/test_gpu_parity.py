@@ -243,3 +243,18 @@ def test_trajectory_file_rows(nb, tmp_path):
             assert row[0] == t
             np.testing.assert_array_equal(row[1:].reshape(-1, 3), p)
         sim.close()
+
+
+def test_list_capacity_retry_small_theta(nb, oracle):
+    """theta = 0.2 makes the near-field lists ~15x the first capacity guess: the lists are rebuilt
+    with doubled capacities until they fit, and come out identical to the oracle's."""
+    pos, vel, m = ics.plummer(4096, seed=39)
+    sim = nb.CudaSimulation.from_arrays(pos, vel, m, m, precision=nb.PREC_MIXED, order=3, leaf_capacity=8,
+                                        fixed_box=0, theta=0.2, eps=0.01)
+    acc = sim.forces()
+    t = oracle.Tree(pos, m, m, cap=8).traverse(0.2)
+    assert _set(sim.interactions("p2p")) == _set(t.pairs("p2p"))
+    assert _set(sim.interactions("m2l")) == _set(t.pairs("m2l"))
+    a_ref, _ = t.fmm(3, 0.01)
+    assert _rel_rms(acc, a_ref) < 3e-6
+    assert sim.stats()["p2p_leaf_pairs"] == len(t.pairs("p2p"))
