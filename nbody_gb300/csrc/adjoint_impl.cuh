@@ -268,27 +268,34 @@ __device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE
                     for (int j = 0; j < TPL; ++j)
 #pragma unroll
                         for (int qq = 0; qq < 8; ++qq) p[j][qq] = 0;
+                    // one pair: SELF compares the source with the target's own slot (only the round
+                    // that holds the target leaf itself pays for it)
+                    auto pairs = [&](auto self_tag) {
+                        constexpr bool SELF = decltype(self_tag)::value;
 #pragma unroll 1
-                    for (int e = 0; e < nj; ++e) {
-                        const S4 sx = gx_t[e], sv = gn_t[e];
+                        for (int e = 0; e < nj; ++e) {
+                            const S4 sx = gx_t[e], sv = gn_t[e];
 #pragma unroll
-                        for (int j = 0; j < TPL; ++j) {
-                            const S rx = sx.x - xs[j][0], ry = sx.y - xs[j][1], rz = sx.z - xs[j][2];
-                            S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
-                            if (GUARD) s2 = s2 > S(0) ? s2 : S(1e30);
-                            S inv = GUARD ? nb_rsqrt(s2) : nb_rsqrt_n(s2);
-                            if (e == selfe[j]) inv = S(0);
-                            const S inv2 = inv * inv, inv3 = inv2 * inv, inv5 = inv3 * inv2;
-                            const S dl = nb_fma(sv.x, rx, nb_fma(sv.y, ry, sv.z * rz));
-                            const S dk = nb_fma(nk[j].x, rx, nb_fma(nk[j].y, ry, nk[j].z * rz));
-                            const S t = nb_fma(y[j].w, dl, -sx.w * dk) * inv5;
-                            p[j][0] = nb_fma(sv.x, inv3, p[j][0]); p[j][1] = nb_fma(sv.y, inv3, p[j][1]);
-                            p[j][2] = nb_fma(sv.z, inv3, p[j][2]); p[j][3] = nb_fma(sx.w, inv3, p[j][3]);
-                            p[j][4] = nb_fma(rx, t, p[j][4]); p[j][5] = nb_fma(ry, t, p[j][5]);
-                            p[j][6] = nb_fma(rz, t, p[j][6]);
-                            p[j][7] = nb_fma(dl, inv3, p[j][7]);
+                            for (int j = 0; j < TPL; ++j) {
+                                const S rx = sx.x - xs[j][0], ry = sx.y - xs[j][1], rz = sx.z - xs[j][2];
+                                S s2 = nb_fma(rx, rx, nb_fma(ry, ry, nb_fma(rz, rz, eps2)));
+                                if (GUARD) s2 = s2 > S(0) ? s2 : S(1e30);
+                                S inv = GUARD ? nb_rsqrt(s2) : nb_rsqrt_n(s2);
+                                if (SELF && e == selfe[j]) inv = S(0);
+                                const S inv2 = inv * inv, inv3 = inv2 * inv, inv5 = inv3 * inv2;
+                                const S dl = nb_fma(sv.x, rx, nb_fma(sv.y, ry, sv.z * rz));
+                                const S dk = nb_fma(nk[j].x, rx, nb_fma(nk[j].y, ry, nk[j].z * rz));
+                                const S t = nb_fma(y[j].w, dl, -sx.w * dk) * inv5;
+                                p[j][0] = nb_fma(sv.x, inv3, p[j][0]); p[j][1] = nb_fma(sv.y, inv3, p[j][1]);
+                                p[j][2] = nb_fma(sv.z, inv3, p[j][2]); p[j][3] = nb_fma(sx.w, inv3, p[j][3]);
+                                p[j][4] = nb_fma(rx, t, p[j][4]); p[j][5] = nb_fma(ry, t, p[j][5]);
+                                p[j][6] = nb_fma(rz, t, p[j][6]);
+                                p[j][7] = nb_fma(dl, inv3, p[j][7]);
+                            }
                         }
-                    }
+                    };
+                    if (__any_sync(0xffffffffu, self)) pairs(std::true_type());
+                    else pairs(std::false_type());
 #pragma unroll
                     for (int j = 0; j < TPL; ++j)
 #pragma unroll
