@@ -274,17 +274,29 @@ __global__ void __launch_bounds__(256) k_lv_totals(CompactArgs A) {
 }
 
 // Moves the entries of multi-block targets behind the staged ones, one destination entry per
-// thread: the target by binary search over the moved-entry offsets, then its block by walking its
-// rows in level order.  Parallel over entries, so a long list (a large leaf with partners on many
-// levels) does not serialise on one warp.
-__device__ __forceinline__ void move_entry(const CompactArgs& A, uint32_t d, const uint32_t* cpo, const uint32_t* soff,
-                                           const uint32_t* scnt, uint32_t* list, uint32_t base, uint32_t* off) {
-    int lo = 0, hi = A.nn;                      // largest t with cpo[t] <= d
+// lane: a warp takes 32 consecutive destinations, finds the target of its first one by binary search
+// over the moved-entry offsets (lanes past that target's end search for their own), then each lane
+// walks its target's rows in level order to its source entry.  Parallel over entries, so a long
+// list (a large leaf with partners on many levels) does not serialise on one warp.
+__device__ __forceinline__ int moved_target(const uint32_t* cpo, int nn, uint32_t d) {
+    int lo = 0, hi = nn;                        // largest t with cpo[t] <= d
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
         if (cpo[mid] <= d) lo = mid; else hi = mid;
     }
-    const int t = lo;
+    return lo;
+}
+
+__device__ __forceinline__ void move_entries(const CompactArgs& A, uint32_t d0, uint32_t tot, const uint32_t* cpo,
+                                             const uint32_t* soff, const uint32_t* scnt, uint32_t* list, uint32_t base,
+                                             uint32_t* off) {
+    const int lane = lane_id();
+    int t0 = 0;
+    if (lane == 0) t0 = moved_target(cpo, A.nn, d0);
+    t0 = __shfl_sync(0xffffffffu, t0, 0);
+    const uint32_t d = d0 + lane;
+    if (d >= tot) return;
+    const int t = d < cpo[t0 + 1] ? t0 : moved_target(cpo, A.nn, d);
     uint32_t k = d - cpo[t];
     if (k == 0) off[t] = base + cpo[t];
     const NodeRec nd = A.nodes[t];
@@ -309,10 +321,12 @@ __global__ void __launch_bounds__(256) k_lv_move(CompactArgs A) {
             atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_M2L_CAP | NB_ERRBIT_P2P_CAP);
         return;
     }
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < tot_m + tot_p; d += stride) {
-        if (d < tot_m) move_entry(A, d, A.m2l_cpo, A.m2l_soff, A.m2l_scnt, A.m2l_list, em, A.m2l_off);
-        else move_entry(A, d - tot_m, A.p2p_cpo, A.p2p_soff, A.p2p_scnt, A.p2p_list, ep, A.p2p_off);
+    // warp-sized chunks of destinations: far-field chunks first, then near-field ones
+    const uint32_t cm = (tot_m + 31) / 32, cp = (tot_p + 31) / 32;
+    const uint32_t stride = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < cm + cp; w += stride) {
+        if (w < cm) move_entries(A, 32 * w, tot_m, A.m2l_cpo, A.m2l_soff, A.m2l_scnt, A.m2l_list, em, A.m2l_off);
+        else move_entries(A, 32 * (w - cm), tot_p, A.p2p_cpo, A.p2p_soff, A.p2p_scnt, A.p2p_list, ep, A.p2p_off);
     }
 }
 

@@ -76,12 +76,18 @@ __global__ void __launch_bounds__(TB) k_kick_drift_bbox(int64_t n, StatePtrs<R> 
             mn[d] = fmin(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
             mx[d] = fmax(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
         }
-    if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            atomicMin(&bbox[d], ord_key(mn[d]));
-            atomicMax(&bbox[3 + d], ord_key(mx[d]));
-        }
+    // block reduction, then one atomic per bound per block (per-warp atomics on six words serialise)
+    __shared__ double s_mn[TB / 32][3], s_mx[TB / 32][3];
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int d = 0; d < 3; ++d) { s_mn[warp][d] = mn[d]; s_mx[warp][d] = mx[d]; }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int d = threadIdx.x;
+        double a = s_mn[0][d], b = s_mx[0][d];
+        for (int w = 1; w < TB / 32; ++w) { a = fmin(a, s_mn[w][d]); b = fmax(b, s_mx[w][d]); }
+        atomicMin(&bbox[d], ord_key(a));
+        atomicMax(&bbox[3 + d], ord_key(b));
     }
     if (bad) atomicOr((unsigned int*)&info[INFO_ERR], NB_ERRBIT_NONFINITE);
 }
@@ -298,7 +304,7 @@ int begin_step_t(nbody_ctx* c, int kdk) {
     NB_CU(c, cudaMemsetAsync(bb, 0xff, 3 * sizeof(unsigned long long), c->st));
     NB_CU(c, cudaMemsetAsync(bb + 3, 0x00, 3 * sizeof(unsigned long long), c->st));
     unsigned g = nblk(n);
-    if (g > 4096) g = 4096;
+    if (g > 152 * 8) g = 152 * 8;
     if (g == 0) g = 1;
     k_kick_drift_bbox<R><<<g, TB, 0, c->st>>>(n, state<R>(c, c->cur), 0.5 * c->prm.dt, c->prm.dt, kdk, bb,
                                               DP<int32_t>(c->info));
