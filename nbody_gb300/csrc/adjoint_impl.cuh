@@ -186,10 +186,11 @@ __device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE
     constexpr bool KH = Prec<MODE>::kahan;
     constexpr int NG = 32 / CT;
     constexpr int TILE = P2P_WTILE / NG < 32 ? P2P_WTILE / NG : 32;
+    static_assert(NG * (TILE + 1) <= P2P_WROWS, "group tiles exceed the warp's shared rows");
     const int lane = lane_id();
     const int grp = lane / CT, gl = lane % CT;
-    S4* gx_t = tx + grp * TILE;
-    S4* gn_t = tn + grp * TILE;
+    S4* gx_t = tx + grp * (TILE + 1);
+    S4* gn_t = tn + grp * (TILE + 1);
     const double unit = A.box->unit;
     const S4* src = (const S4*)A.src;
     const S4* nu = (const S4*)A.nu;
@@ -336,8 +337,8 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS, AdjShape<CLS>::TPL == 3 ? 3 : 
     k_adj_p2p(AdjP2PArgs A, int64_t li_lo, int64_t li_hi, uint32_t w_lo, uint32_t w_hi) {
     typedef typename Prec<MODE>::S4 S4;
     constexpr int CT = AdjShape<CLS>::CT, TPL = AdjShape<CLS>::TPL;
-    __shared__ S4 tx[ADJ_WARPS][P2P_WTILE];
-    __shared__ S4 tn[ADJ_WARPS][P2P_WTILE];
+    __shared__ S4 tx[ADJ_WARPS][P2P_WROWS];
+    __shared__ S4 tn[ADJ_WARPS][P2P_WROWS];
     const int wib = threadIdx.x >> 5;
     const uint32_t w = w_lo + blockIdx.x * ADJ_WARPS + wib;
     if (w >= w_hi) return;

@@ -561,6 +561,9 @@ template <> struct P2PShape<3> { static constexpr int CT = 16, TPL = 2; };
 template <> struct P2PShape<4> { static constexpr int CT = 16, TPL = 3; };
 template <> struct P2PShape<5> { static constexpr int CT = 32, TPL = 2; };
 constexpr int P2P_WTILE = 128;    // shared source entries per warp (groups x entries per group)
+// shared rows per warp: each group's tile is followed by one pad entry, so the groups of a half-warp
+// (which read different entries in the same step) fall in distinct shared-memory banks
+constexpr int P2P_WROWS = P2P_WTILE + 8;
 
 // which leaf / chunk a near-field work item is: last li in [lo, hi) with work_off[li] <= w
 __device__ __forceinline__ int64_t p2p_leaf_of(const uint32_t* work_off, int64_t lo, int64_t hi, uint32_t w) {
@@ -587,9 +590,10 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
     constexpr int NG = 32 / CT;
     constexpr int TILE = P2P_WTILE / NG < 32 ? P2P_WTILE / NG : 32;
     constexpr int EPL = TILE / CT;          // tile entries each lane loads
+    static_assert(NG * (TILE + 1) <= P2P_WROWS, "group tiles exceed the warp's shared rows");
     const int lane = lane_id();
     const int grp = lane / CT, gl = lane % CT;
-    S4* gtile = tile + grp * TILE;
+    S4* gtile = tile + grp * (TILE + 1);
     const double unit = A.box->unit;
     const S4* src = (const S4*)A.src;
     const uint32_t cnt_t = nt.count;
@@ -744,7 +748,7 @@ __global__ void __launch_bounds__(32 * P2P_WARPS, P2PShape<CLS>::TPL == 3 ? 4 : 
     typedef typename Prec<MODE>::S4 S4;
     constexpr int T = nb_terms<P>::value;
     constexpr int CT = P2PShape<CLS>::CT, TPL = P2PShape<CLS>::TPL;
-    __shared__ S4 tile[P2P_WARPS][P2P_WTILE];
+    __shared__ S4 tile[P2P_WARPS][P2P_WROWS];
     __shared__ S sL[P2P_WARPS][T];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
     const uint32_t w = w_lo + blockIdx.x * P2P_WARPS + wib;

@@ -548,6 +548,7 @@ int nb_build_lists(nbody_ctx* c) {
         // extent of each list buffer (staged entries plus the moved ones)
         c->h_info[INFO_M2L_TAIL] = c->h_info[INFO_BASE_M2L] + c->h_info[INFO_LVL_M2L] + c->h_info[INFO_MOVED_M2L];
         c->h_info[INFO_P2P_TAIL] = c->h_info[INFO_BASE_P2P] + c->h_info[INFO_LVL_P2P] + c->h_info[INFO_MOVED_P2P];
+        if (c->h_info[INFO_SCAN_ERR]) return nb_fail(c, NBODY_ERR_CUDA, "a device scan did not complete in time");
         const uint32_t e = (uint32_t)c->h_info[INFO_ERR];
         const uint32_t caps = NB_ERRBIT_PEND_CAP | NB_ERRBIT_P2P_CAP | NB_ERRBIT_M2L_CAP | NB_ERRBIT_ITEM_CAP;
         if (!(e & caps)) return NBODY_OK;

@@ -61,6 +61,7 @@ enum {
     INFO_ITEMS1 = 40,              // list-building items of the current level plus one (scan length)
     INFO_CLS_LEAF = 48,            // 48 .. 54: first leaf (in near-field order) of each class, then the count
     INFO_CLS_WORK = 56,            // 56 .. 62: first near-field work item of each class, then the total
+    INFO_SCAN_ERR = 63,            // sticky: a device scan's look-back gave up waiting (never cleared by a step)
     INFO_WORDS = 64
 };
 
@@ -116,7 +117,9 @@ struct nbody_ctx {
     DevBuf pot;                    // potential per particle (diagnostics)
 
     // sort scratch
-    DevBuf keys[2], vals[2], hist, hist_scan, scan_part;
+    DevBuf keys[2], vals[2], hist, hist_scan;
+    DevBuf scan_part;              // single-pass scan state: ticket counter and tile status words
+    uint64_t scan_epoch = 0;       // tag of the last scan's status words
 
     // tree scratch and result
     DevBuf cpl, wnd, leaflvl, nc, pfx, seedk[2], seedv[2], nodes, leafflag, leafpfx, leaves;

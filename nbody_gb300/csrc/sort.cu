@@ -35,55 +35,27 @@ __device__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
     return r;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t* __restrict__ in, int64_t n,
-                                                                uint32_t* __restrict__ part) {
-    int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
-    uint32_t s = 0;
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; ++k)
-        if (base + k < n) s += in[base + k];
-    uint32_t tot;
-    block_excl_scan(s, &tot);
-    if (threadIdx.x == 0) part[blockIdx.x] = tot;
-}
+// Single-pass exclusive scan over up to three arrays (decoupled look-back).  Each block takes
+// its tile from a ticket counter, so every tile it waits on belongs to a block that is already
+// running (the block that draws the last ticket puts the counter back to zero for the next
+// launch); it publishes its tile's sum, then walks back over the status words of the tiles
+// before it (one warp per array, 32 tiles per step) until it meets an inclusive prefix.  A
+// status word packs the call's epoch, a flag (1: tile sum, 2: inclusive prefix) and the value
+// in one 64-bit store, so words left by earlier calls never match and no reset is needed.  The
+// sums are integer, so the result does not depend on which words a block happened to see.
+constexpr uint32_t SCAN_EPOCH_SHIFT = 34;
+constexpr uint64_t SCAN_FLAG_SUM = 1ull << 32, SCAN_FLAG_INCL = 2ull << 32;
+constexpr int SCAN_SPIN_LIMIT = 1 << 20;        // polls of one status word before giving up (~1 s)
 
-__global__ void __launch_bounds__(1024) k_scan_partials(uint32_t* part, int64_t nb, uint32_t* total) {
-    uint32_t run = 0;
-    for (int64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
-        int64_t i = b0 + threadIdx.x;
-        uint32_t v = i < nb ? part[i] : 0u;
-        uint32_t tot;
-        uint32_t e = block_excl_scan(v, &tot);
-        if (i < nb) part[i] = run + e;
-        run += tot;
-    }
-    if (threadIdx.x == 0 && total) *total = run;
-}
-
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
-                                                              int64_t n, const uint32_t* __restrict__ part) {
-    int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
-    uint32_t v[SCAN_ITEMS];
-    uint32_t s = 0;
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; ++k) {
-        v[k] = base + k < n ? in[base + k] : 0u;
-        s += v[k];
-    }
-    uint32_t e = block_excl_scan(s, nullptr) + part[blockIdx.x];
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; ++k) {
-        if (base + k < n) out[base + k] = e;
-        e += v[k];
-    }
-}
-
-// the same three phases over K arrays at once (one launch per phase for all of them)
 struct ScanK {
     const uint32_t* in[3];         // null: array unused
     uint32_t* out[3];
     uint32_t* total[3];
     const uint32_t* n_dev;         // non-null: scan only the first *n_dev entries (<= n)
+    unsigned long long* state;     // [0] ticket counter, [1 + a * nb + t] status of tile t of array a
+    int64_t nb;                    // blocks of this launch (tiles of n entries)
+    uint64_t epoch;
+    int32_t* info;                 // INFO_SCAN_ERR is raised when a look-back gives up
 };
 
 __device__ __forceinline__ int64_t scan_len(const ScanK& A, int64_t n) {
@@ -92,68 +64,106 @@ __device__ __forceinline__ int64_t scan_len(const ScanK& A, int64_t n) {
     return m < n ? m : n;
 }
 
-template <int K>
-__global__ void __launch_bounds__(SCAN_THREADS) k_scank_reduce(ScanK A, int64_t n, uint32_t* __restrict__ part,
-                                                                 int64_t nb) {
-    n = scan_len(A, n);
-    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
-    if ((int64_t)blockIdx.x * SCAN_TILE >= n) {
-        if (threadIdx.x < K) part[threadIdx.x * nb + blockIdx.x] = 0;
-        return;
-    }
-#pragma unroll
-    for (int a = 0; a < K; ++a) {
-        if (!A.in[a]) continue;
-        uint32_t s = 0;
-#pragma unroll
-        for (int k = 0; k < SCAN_ITEMS; ++k)
-            if (base + k < n) s += A.in[a][base + k];
-        uint32_t tot;
-        block_excl_scan(s, &tot);
-        if (threadIdx.x == 0) part[a * nb + blockIdx.x] = tot;
-    }
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
 }
 
-template <int K>
-__global__ void __launch_bounds__(1024) k_scank_partials(ScanK A, uint32_t* part, int64_t nb) {
-#pragma unroll
-    for (int a = 0; a < K; ++a) {
-        if (!A.in[a]) continue;
-        uint32_t run = 0;
-        for (int64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
-            const int64_t i = b0 + threadIdx.x;
-            const uint32_t v = i < nb ? part[a * nb + i] : 0u;
-            uint32_t tot;
-            const uint32_t e = block_excl_scan(v, &tot);
-            if (i < nb) part[a * nb + i] = run + e;
-            run += tot;
+// one warp: publishes tile t's sum `agg`, returns the sum of all tiles before t (every lane)
+__device__ uint32_t scan_lookback(unsigned long long* st, int64_t t, uint32_t agg, uint64_t epoch, int32_t* info) {
+    const int lane = lane_id();
+    const unsigned long long tag = epoch << SCAN_EPOCH_SHIFT;
+    if (t == 0) {
+        if (lane == 0) st_relaxed_u64(st, tag | SCAN_FLAG_INCL | agg);
+        return 0;
+    }
+    if (lane == 0) st_relaxed_u64(st + t, tag | SCAN_FLAG_SUM | agg);
+    uint32_t prefix = 0;
+    bool gave_up = false;
+    for (int64_t j = t - 1;; j -= 32) {
+        const int64_t my = j - lane;
+        // positions before tile 0 read as an inclusive zero; tile 0 itself is always inclusive
+        uint64_t flag = SCAN_FLAG_INCL;
+        uint32_t val = 0;
+        if (my >= 0) {
+            unsigned long long w = ld_relaxed_u64(st + my);
+            int spins = 0;
+            while ((w >> SCAN_EPOCH_SHIFT) != epoch && ++spins < SCAN_SPIN_LIMIT) {
+                __nanosleep(64);
+                w = ld_relaxed_u64(st + my);
+            }
+            if ((w >> SCAN_EPOCH_SHIFT) == epoch) {
+                flag = w & (3ull << 32);
+                val = (uint32_t)w;
+            } else {
+                gave_up = true;
+            }
         }
-        if (threadIdx.x == 0 && A.total[a]) *A.total[a] = run;
+        const unsigned incl = __ballot_sync(0xffffffffu, flag == SCAN_FLAG_INCL);
+        const int stop = incl ? __ffs(incl) - 1 : 31;
+        uint32_t s = lane <= stop ? val : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        prefix += s;
+        if (incl) break;
     }
+    if (__any_sync(0xffffffffu, gave_up) && lane == 0) atomicOr((unsigned int*)&info[INFO_SCAN_ERR], 1u);
+    if (lane == 0) st_relaxed_u64(st + t, tag | SCAN_FLAG_INCL | (uint32_t)(prefix + agg));
+    return prefix;
 }
 
 template <int K>
-__global__ void __launch_bounds__(SCAN_THREADS) k_scank_down(ScanK A, int64_t n, const uint32_t* __restrict__ part,
-                                                               int64_t nb) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(ScanK A, int64_t n) {
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_prefix[K];
     n = scan_len(A, n);
-    if ((int64_t)blockIdx.x * SCAN_TILE >= n) return;
-    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    const int64_t last = n > 0 ? (n - 1) / SCAN_TILE : 0;     // the tile that writes the totals
+    if ((int64_t)blockIdx.x > last) return;                    // only last + 1 blocks draw tickets
+    if (threadIdx.x == 0) {
+        const unsigned long long tk = atomicAdd(A.state, 1ull);
+        if (tk == (unsigned long long)last) atomicExch(A.state, 0ull);
+        if (tk > (unsigned long long)last) atomicOr((unsigned int*)&A.info[INFO_SCAN_ERR], 2u);
+        s_tile = tk > (unsigned long long)last ? 0xffffffffu : (uint32_t)tk;
+    }
+    __syncthreads();
+    if (s_tile == 0xffffffffu) return;                         // counter left over by a failed launch
+    const int64_t t = s_tile;
+    const int64_t base = t * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[K][SCAN_ITEMS], ex[K], agg[K];
 #pragma unroll
     for (int a = 0; a < K; ++a) {
+        ex[a] = agg[a] = 0;
         if (!A.in[a]) continue;
-        uint32_t v[SCAN_ITEMS];
         uint32_t s = 0;
 #pragma unroll
         for (int k = 0; k < SCAN_ITEMS; ++k) {
-            v[k] = base + k < n ? A.in[a][base + k] : 0u;
-            s += v[k];
+            v[a][k] = base + k < n ? A.in[a][base + k] : 0u;
+            s += v[a][k];
         }
-        uint32_t e = block_excl_scan(s, nullptr) + part[a * nb + blockIdx.x];
+        ex[a] = block_excl_scan(s, &agg[a]);
+    }
+    const int warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int a = 0; a < K; ++a)
+        if (warp == a && A.in[a]) {
+            const uint32_t pre = scan_lookback(A.state + 1 + a * A.nb, t, agg[a], A.epoch, A.info);
+            if (lane_id() == 0) s_prefix[a] = pre;
+        }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        if (!A.in[a]) continue;
+        uint32_t e = s_prefix[a] + ex[a];
 #pragma unroll
         for (int k = 0; k < SCAN_ITEMS; ++k) {
             if (base + k < n) A.out[a][base + k] = e;
-            e += v[k];
+            e += v[a][k];
         }
+        if (t == last && threadIdx.x == 0 && A.total[a]) *A.total[a] = s_prefix[a] + agg[a];
     }
 }
 
@@ -218,20 +228,44 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_scatter(const uint64_t*
 
 }  // namespace
 
+namespace {
+
+// launches the single-pass scan over the arrays of `in` (null entries skipped)
+template <int K>
+int scan_launch(nbody_ctx* c, const uint32_t* const* in, uint32_t* const* out, int64_t n, uint32_t* const* total,
+                const uint32_t* n_dev) {
+    const int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    const size_t bytes = sizeof(unsigned long long) * (size_t)(1 + K * nb);
+    if (c->scan_part.bytes < bytes) {
+        NB_TRY(nb_grow(c, c->scan_part, bytes));
+        NB_CU(c, cudaMemsetAsync(c->scan_part.p, 0, c->scan_part.bytes, c->st));
+    }
+    ScanK A;
+    for (int a = 0; a < 3; ++a) {
+        A.in[a] = a < K ? in[a] : nullptr;
+        A.out[a] = a < K ? out[a] : nullptr;
+        A.total[a] = a < K ? total[a] : nullptr;
+    }
+    A.n_dev = n_dev;
+    A.state = DP<unsigned long long>(c->scan_part);
+    A.nb = nb;
+    c->scan_epoch = c->scan_epoch % ((1ull << 30) - 1) + 1;     // 1 .. 2^30 - 1; 0 marks a cleared word
+    A.epoch = c->scan_epoch;
+    A.info = DP<int32_t>(c->info);
+    k_scan<K><<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(A, n);
+    NB_LAUNCHED(c, "scan");
+    c->launches += 1;
+    return NBODY_OK;
+}
+
+}  // namespace
+
 int nb_scan_u32(nbody_ctx* c, const uint32_t* in, uint32_t* out, int64_t n, uint32_t* total_dev) {
     if (n <= 0) {
         if (total_dev) NB_CU(c, cudaMemsetAsync(total_dev, 0, sizeof(uint32_t), c->st));
         return NBODY_OK;
     }
-    int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
-    NB_TRY(nb_grow(c, c->scan_part, sizeof(uint32_t) * (size_t)(nb + 1)));
-    uint32_t* part = DP<uint32_t>(c->scan_part);
-    k_scan_reduce<<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(in, n, part);
-    k_scan_partials<<<1, 1024, 0, c->st>>>(part, nb, total_dev);
-    k_scan_down<<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(in, out, n, part);
-    NB_LAUNCHED(c, "scan");
-    c->launches += 3;
-    return NBODY_OK;
+    return scan_launch<1>(c, &in, &out, n, &total_dev, nullptr);
 }
 
 int nb_scan3_u32(nbody_ctx* c, const uint32_t* const in[3], uint32_t* const out[3], int64_t n,
@@ -241,18 +275,8 @@ int nb_scan3_u32(nbody_ctx* c, const uint32_t* const in[3], uint32_t* const out[
             if (total_dev[a]) NB_CU(c, cudaMemsetAsync(total_dev[a], 0, sizeof(uint32_t), c->st));
         return NBODY_OK;
     }
-    const int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
-    NB_TRY(nb_grow(c, c->scan_part, sizeof(uint32_t) * (size_t)(3 * nb + 1)));
-    uint32_t* part = DP<uint32_t>(c->scan_part);
-    ScanK A;
-    for (int a = 0; a < 3; ++a) { A.in[a] = in[a]; A.out[a] = out[a]; A.total[a] = total_dev[a]; }
-    A.n_dev = n_dev;
-    k_scank_reduce<3><<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(A, n, part, nb);
-    k_scank_partials<3><<<1, 1024, 0, c->st>>>(A, part, nb);
-    k_scank_down<3><<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(A, n, part, nb);
-    NB_LAUNCHED(c, "scan3");
-    c->launches += 3;
-    return NBODY_OK;
+    if (!in[2]) return scan_launch<2>(c, in, out, n, total_dev, n_dev);
+    return scan_launch<3>(c, in, out, n, total_dev, n_dev);
 }
 
 int nb_radix_sort(nbody_ctx* c, int64_t n, uint64_t* k0, uint32_t* v0, uint64_t* k1, uint32_t* v1, int begin_bit,

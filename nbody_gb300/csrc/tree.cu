@@ -348,7 +348,7 @@ int nb_build_tree(nbody_ctx* c) {
     const int64_t n = c->n;
     const int C = c->prm.leaf_capacity;
     int32_t* info = DP<int32_t>(c->info);
-    NB_CU(c, cudaMemsetAsync(info + INFO_DEPTH, 0, sizeof(int32_t) * (INFO_WORDS - INFO_DEPTH), c->st));
+    NB_CU(c, cudaMemsetAsync(info + INFO_DEPTH, 0, sizeof(int32_t) * (INFO_SCAN_ERR - INFO_DEPTH), c->st));
     k_tree_cpl<<<nblk(n), TB, 0, c->st>>>(n, C, DP<uint64_t>(c->keys[0]), DP<int32_t>(c->cpl), DP<int32_t>(c->wnd));
     k_tree_chain<<<nblk(n), TB, 0, c->st>>>(n, C, c->prm.max_level, DP<int32_t>(c->cpl), DP<int32_t>(c->wnd),
                                             DP<uint32_t>(c->nc), info);
@@ -357,6 +357,7 @@ int nb_build_tree(nbody_ctx* c) {
     NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->nc), DP<uint32_t>(c->pfx), n, (uint32_t*)(info + INFO_NNODES)));
     NB_CU(c, cudaMemcpyAsync(c->h_info, info, sizeof(int32_t) * INFO_WORDS, cudaMemcpyDeviceToHost, c->st));
     NB_CU(c, cudaStreamSynchronize(c->st));
+    if (c->h_info[INFO_SCAN_ERR]) return nb_fail(c, NBODY_ERR_CUDA, "a device scan did not complete in time");
     if ((uint32_t)c->h_info[INFO_ERR] & NB_ERRBIT_NONFINITE)
         return nb_fail(c, NBODY_ERR_STATE, "non-finite particle position");
     c->nnodes = (uint32_t)c->h_info[INFO_NNODES];
