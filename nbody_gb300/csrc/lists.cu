@@ -37,7 +37,9 @@ struct LevelArgs {
     const uint32_t *pin_off, *pin_cnt, *pin_list;     // pending input (level r - 1)
     uint32_t *pout_off, *pout_cnt, *pout_list;        // pending output (level r)
     uint32_t pend_cap;
-    uint32_t *nch, *first, *target;                   // items: chunks per target, first item, item -> target
+    uint32_t *nch, *first;                            // per target: chunks (items), first item
+    uint4* item;                                      // per item: target, input offset, input count, chunks
+                                                      // of the target (first item only, else 0)
     uint32_t item_cap;
     uint32_t* cnt[3];                                 // per item: far, near, pending outputs
     uint32_t* off[3];                                 // their exclusive scans
@@ -92,6 +94,8 @@ __global__ void k_lv_plan(LevelArgs A) {
     A.p2p_scnt[t] = 0;
 }
 
+// the item records of every active target: one item per chunk of 32 input partners, so the item
+// kernels start from one 16-byte load instead of a chain of dependent ones
 __global__ void k_lv_fill(LevelArgs A) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= A.hi) return;
@@ -101,31 +105,33 @@ __global__ void k_lv_fill(LevelArgs A) {
         atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_ITEM_CAP);
         return;
     }
-    for (uint32_t c = 0; c < n; ++c) A.target[f + c] = (uint32_t)t;
+    uint32_t off, cnt;
+    target_input(A, (uint32_t)t, A.nodes[t], off, cnt);
+    for (uint32_t c = 0; c < n; ++c)
+        A.item[f + c] = make_uint4((uint32_t)t, off + 32 * c, min(32u, cnt - 32 * c), c == 0 ? n : 0u);
 }
 
 // Classifies the candidates of item i once: each goes to row i of the staging table (candidate
 // order, class in the top two bits: 1 far field, 2 near field, 3 pending) and the item's three
 // counts are kept for the scans; k_lv_scatter then places the row's entries.
+constexpr int CLS_UNROLL = 4;         // candidate groups of 32 whose node records are loaded together
+
 __device__ void lv_classify(const LevelArgs& A, uint32_t i, uint32_t* cand) {
     const int lane = lane_id();
-    const uint32_t t = A.target[i];
-    const NodeRec nt = A.nodes[t];
-    const bool tleaf = nt.nchild == 0;
-    int tcx, tcy, tcz;
-    centre_fine32(nt, tcx, tcy, tcz);
-    const float tw = (float)(1u << (NB_LEVELS + 1 - nt.level));
-    uint32_t poff, pcnt;
-    target_input(A, t, nt, poff, pcnt);
-    const uint32_t chunk = i - A.first[t];
-    const uint32_t j = chunk * 32 + lane;
+    const uint4 it = A.item[i];
+    const uint32_t t = it.x;
     uint32_t s = NONE, ns = 0, cb = 0;
-    if (j < pcnt) {
-        s = A.pin_list[poff + j];
+    if ((uint32_t)lane < it.z) s = A.pin_list[it.y + lane];
+    const NodeRec nt = A.nodes[t];
+    if (s != NONE) {
         const NodeRec sn = A.nodes[s];
         ns = sn.nchild ? sn.nchild : 1u;
         cb = sn.nchild ? (uint32_t)sn.child_begin : s;
     }
+    const bool tleaf = nt.nchild == 0;
+    int tcx, tcy, tcz;
+    centre_fine32(nt, tcx, tcy, tcz);
+    const float tw = (float)(1u << (NB_LEVELS + 1 - nt.level));
     const uint32_t inc = warp_incl_scan(ns);
     const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
     for (uint32_t u = 0; u < ns; ++u) cand[inc - ns + u] = cb + u;
@@ -133,22 +139,30 @@ __device__ void lv_classify(const LevelArgs& A, uint32_t i, uint32_t* cand) {
     uint32_t* row = A.rows + (size_t)i * CANDS;
     uint32_t nm = 0, np = 0, nq = 0;
     unsigned long long near_particles = 0;
-    for (uint32_t g = 0; g < total; g += 32) {
-        const uint32_t sc = g + lane < total ? cand[g + lane] : NONE;
-        const bool valid = sc != NONE;
-        NodeRec sn;
-        sn.nchild = 0;
-        sn.count = 0;
-        if (valid) sn = A.nodes[sc];
-        const bool approx = valid && sc != t && mac_f32(tcx, tcy, tcz, tw, sn, A.theta2);
-        const bool sleaf = valid && sn.nchild == 0;
-        const bool near = valid && !approx && tleaf && sleaf;
-        const bool pend = valid && !approx && !near;
-        if (valid) row[g + lane] = sc | ((approx ? 1u : near ? 2u : 3u) << 30);
-        if (near) near_particles += sn.count;
-        nm += __popc(__ballot_sync(0xffffffffu, approx));
-        np += __popc(__ballot_sync(0xffffffffu, near));
-        nq += __popc(__ballot_sync(0xffffffffu, pend));
+    for (uint32_t g0 = 0; g0 < total; g0 += 32 * CLS_UNROLL) {
+        uint32_t sc[CLS_UNROLL];
+        NodeRec sn[CLS_UNROLL];
+#pragma unroll
+        for (int u = 0; u < CLS_UNROLL; ++u) {
+            const uint32_t g = g0 + 32 * u + lane;
+            sc[u] = g < total ? cand[g] : NONE;
+            sn[u].nchild = 0;
+            sn[u].count = 0;
+            if (sc[u] != NONE) sn[u] = A.nodes[sc[u]];
+        }
+#pragma unroll
+        for (int u = 0; u < CLS_UNROLL; ++u) {
+            const bool valid = sc[u] != NONE;
+            const bool approx = valid && sc[u] != t && mac_f32(tcx, tcy, tcz, tw, sn[u], A.theta2);
+            const bool sleaf = valid && sn[u].nchild == 0;
+            const bool near = valid && !approx && tleaf && sleaf;
+            const bool pend = valid && !approx && !near;
+            if (valid) row[g0 + 32 * u + lane] = sc[u] | ((approx ? 1u : near ? 2u : 3u) << 30);
+            if (near) near_particles += sn[u].count;
+            nm += __popc(__ballot_sync(0xffffffffu, approx));
+            np += __popc(__ballot_sync(0xffffffffu, near));
+            nq += __popc(__ballot_sync(0xffffffffu, pend));
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) near_particles += __shfl_xor_sync(0xffffffffu, near_particles, o);
@@ -194,9 +208,16 @@ __global__ void __launch_bounds__(32 * LW) k_lv_scatter(LevelArgs A) {
         const uint32_t total = c_m + c_p + c_q;
         const uint32_t* row = A.rows + (size_t)i * CANDS;
         const uint32_t lt = lanemask_lt();
+        const uint4 it = A.item[i];
+        // the whole row at once (CANDS / 32 loads in flight per lane), then placed group by group
+        uint32_t ent[CANDS / 32];
+#pragma unroll
+        for (int u = 0; u < CANDS / 32; ++u) ent[u] = 32 * u + lane < total ? row[32 * u + lane] : 0u;
         uint32_t nm = 0, np = 0, nq = 0;
-        for (uint32_t g = 0; g < total; g += 32) {
-            const uint32_t e = g + lane < total ? row[g + lane] : 0u;
+#pragma unroll
+        for (int u = 0; u < CANDS / 32; ++u) {
+            if (32u * u >= total) break;
+            const uint32_t e = ent[u];
             const uint32_t cl = e >> 30, sc = e & 0x3fffffffu;
             const uint32_t mm = __ballot_sync(0xffffffffu, cl == 1), mp = __ballot_sync(0xffffffffu, cl == 2),
                            mq = __ballot_sync(0xffffffffu, cl == 3);
@@ -208,10 +229,10 @@ __global__ void __launch_bounds__(32 * LW) k_lv_scatter(LevelArgs A) {
             nq += __popc(mq);
         }
         if (lane == 0) {
-            const uint32_t t = A.target[i];
-            if (i == A.first[t]) {
+            const uint32_t t = it.x;
+            if (it.w) {
                 // the target's blocks of this level: its first item's offset, through the end of its last
-                const uint32_t e = i + A.nch[t];
+                const uint32_t e = i + it.w;
                 A.m2l_soff[t] = o_m;
                 A.m2l_scnt[t] = A.off[0][e] - A.off[0][i];
                 A.p2p_soff[t] = o_p;
@@ -416,7 +437,7 @@ int nb_build_lists(nbody_ctx* c) {
         NB_TRY(nb_grow(c, c->pend_list, sizeof(uint32_t) * 2 * c->pend_cap));
         NB_TRY(nb_grow(c, c->p2p_list, sizeof(uint32_t) * c->p2p_cap));
         NB_TRY(nb_grow(c, c->m2l_list, sizeof(uint32_t) * c->m2l_cap));
-        NB_TRY(nb_grow(c, c->lst_target, sizeof(uint32_t) * c->item_cap));
+        NB_TRY(nb_grow(c, c->lst_target, sizeof(uint4) * c->item_cap));
         NB_TRY(nb_grow(c, c->lst_rows, sizeof(uint32_t) * CANDS * c->item_cap));
         NB_TRY(nb_grow(c, c->lst_cnt, sizeof(uint32_t) * 3 * (c->item_cap + 1)));
         NB_TRY(nb_grow(c, c->lst_off, sizeof(uint32_t) * 3 * (c->item_cap + 1)));
@@ -441,7 +462,7 @@ int nb_build_lists(nbody_ctx* c) {
         A.pend_cap = (uint32_t)c->pend_cap;
         A.nch = DP<uint32_t>(c->lst_nch);
         A.first = DP<uint32_t>(c->lst_first);
-        A.target = DP<uint32_t>(c->lst_target);
+        A.item = DP<uint4>(c->lst_target);
         A.item_cap = (uint32_t)c->item_cap;
         A.rows = DP<uint32_t>(c->lst_rows);
         for (int k = 0; k < 3; ++k) { A.cnt[k] = cnt + k * ic; A.off[k] = off + k * ic; }
