@@ -192,7 +192,9 @@ __global__ void __launch_bounds__(128) k_p2m(int64_t nleaves, const uint32_t* __
 }
 
 // ---------------------------------------------------------------------------
-// M2M: one level, warp per internal node
+// M2M: one level, warp per internal node.  The children are shifted CB at a time: their multipoles
+// and shift monomials are staged together, and each lane runs CB independent accumulation chains
+// (one per child) over its coefficients' term pairs, then adds them to its sum in child order.
 // ---------------------------------------------------------------------------
 template <int MODE, int P>
 __global__ void __launch_bounds__(128) k_m2m(int lo, int hi, const NodeRec* __restrict__ nodes,
@@ -200,9 +202,10 @@ __global__ void __launch_bounds__(128) k_m2m(int lo, int hi, const NodeRec* __re
     typedef typename Prec<MODE>::H H;
     constexpr int T = nb_terms<P>::value;
     constexpr int TM = nb_tm<P>::value;
-    __shared__ H sM[4][T];
-    __shared__ H sY[4][T];
-    __shared__ H spw[4][3][P + 1];
+    constexpr int CB = sizeof(H) == 8 ? 4 : 8;      // children per round (shared memory below 48 KB)
+    __shared__ H sM[4][CB][T];
+    __shared__ H sY[4][CB][T];
+    __shared__ H spw[4][CB][3][P + 1];
     const int lane = lane_id(), wib = threadIdx.x >> 5;
     const int k = lo + blockIdx.x * 4 + wib;
     if (k >= hi) return;
@@ -215,27 +218,46 @@ __global__ void __launch_bounds__(128) k_m2m(int lo, int hi, const NodeRec* __re
     H acc[NPL];
 #pragma unroll
     for (int j = 0; j < NPL; ++j) acc[j] = H(0);
-    for (int c = 0; c < nd.nchild; ++c) {
-        const int ch = nd.child_begin + c;
-        const NodeRec cn = nodes[ch];
-        double dx, dy, dz;
-        disp(cn, nd, unit, dx, dy, dz);
-        for (int a = lane; a < T; a += 32) sM[wib][a] = M[(int64_t)ch * TM + a];
-        if (lane < 3) {
-            H d = (H)(lane == 0 ? dx : lane == 1 ? dy : dz), p = H(1);
-            for (int e = 0; e <= P; ++e) { spw[wib][lane][e] = p; p *= d; }
+    for (int c0 = 0; c0 < nd.nchild; c0 += CB) {
+        const int nc = min(CB, (int)nd.nchild - c0);
+        // powers of each child's offset, one lane per (child, axis); absent children shift by zero
+        if (lane < 3 * CB) {
+            const int c = lane / 3, ax = lane - 3 * c;
+            H d = H(0), p = H(1);
+            if (c < nc) {
+                const NodeRec cn = nodes[nd.child_begin + c0 + c];
+                double dx, dy, dz;
+                disp(cn, nd, unit, dx, dy, dz);
+                d = (H)(ax == 0 ? dx : ax == 1 ? dy : dz);
+            }
+            for (int e = 0; e <= P; ++e) { spw[wib][c][ax][e] = p; p *= d; }
+        }
+        for (int idx = lane; idx < CB * T; idx += 32) {
+            const int c = idx / T, a = idx - c * T;
+            sM[wib][c][a] = c < nc ? M[(int64_t)(nd.child_begin + c0 + c) * TM + a] : H(0);
         }
         __syncwarp();
-        for (int a = lane; a < T; a += 32)
-            sY[wib][a] = spw[wib][0][nb_mi[a][0]] * spw[wib][1][nb_mi[a][1]] * spw[wib][2][nb_mi[a][2]] *
-                         (H)nb_invfact[a];
+        for (int idx = lane; idx < CB * T; idx += 32) {
+            const int c = idx / T, a = idx - c * T;
+            sY[wib][c][a] = spw[wib][c][0][nb_mi[a][0]] * spw[wib][c][1][nb_mi[a][1]] * spw[wib][c][2][nb_mi[a][2]] *
+                            (H)nb_invfact[a];
+        }
         __syncwarp();
 #pragma unroll
         for (int j = 0; j < NPL; ++j) {
-            int a = lane + 32 * j;
+            const int a = lane + 32 * j;
             if (a < T) {
+                H sc[CB];
+#pragma unroll
+                for (int c = 0; c < CB; ++c) sc[c] = H(0);
+                for (int u = st[a]; u < st[a + 1]; ++u) {
+                    const int pm = pr[2 * u], py = pr[2 * u + 1];
+#pragma unroll
+                    for (int c = 0; c < CB; ++c) sc[c] = nb_fma(sM[wib][c][pm], sY[wib][c][py], sc[c]);
+                }
                 H s = acc[j];
-                for (int u = st[a]; u < st[a + 1]; ++u) s = nb_fma(sM[wib][pr[2 * u]], sY[wib][pr[2 * u + 1]], s);
+#pragma unroll
+                for (int c = 0; c < CB; ++c) s += sc[c];
                 acc[j] = s;
             }
         }
