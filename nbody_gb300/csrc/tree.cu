@@ -47,11 +47,13 @@ __device__ __forceinline__ double ord_val(unsigned long long k) {
     return __longlong_as_double(b);
 }
 
-// opening kick + drift (leapfrog) and the bounding box of the new positions
+// opening kick + drift (leapfrog) and the bounding box of the new positions.  The box is reduced on
+// order-preserving integer keys of the finite coordinates (integer min/max instead of the FP64 pipe);
+// a non-finite coordinate raises NB_ERRBIT_NONFINITE and stays out of the bounds.
 template <typename R>
 __global__ void __launch_bounds__(TB) k_kick_drift_bbox(int64_t n, StatePtrs<R> s, double hdt, double dt, int kdk,
                                                          unsigned long long* bbox, int32_t* info) {
-    double mn[3] = {1e308, 1e308, 1e308}, mx[3] = {-1e308, -1e308, -1e308};
+    unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
     bool bad = false;
     for (int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x; i < n; i += (int64_t)gridDim.x * TB) {
         R x = s.x[i], y = s.y[i], z = s.z[i];
@@ -61,33 +63,42 @@ __global__ void __launch_bounds__(TB) k_kick_drift_bbox(int64_t n, StatePtrs<R> 
             s.vx[i] = vx; s.vy[i] = vy; s.vz[i] = vz;
             s.x[i] = x; s.y[i] = y; s.z[i] = z;
         }
-        double p[3] = {(double)x, (double)y, (double)z};
+        const double p[3] = {(double)x, (double)y, (double)z};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            bad |= !isfinite(p[d]);
-            mn[d] = fmin(mn[d], p[d]);
-            mx[d] = fmax(mx[d], p[d]);
+            const unsigned long long bits = (unsigned long long)__double_as_longlong(p[d]);
+            const bool nonfinite = (bits & 0x7ff0000000000000ull) == 0x7ff0000000000000ull;
+            bad |= nonfinite;
+            if (nonfinite) continue;          // the bounds cover the finite coordinates only
+            const unsigned long long k = ord_key(p[d]);
+            mn[d] = k < mn[d] ? k : mn[d];
+            mx[d] = k > mx[d] ? k : mx[d];
         }
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            mn[d] = fmin(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
-            mx[d] = fmax(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+            const unsigned long long a = __shfl_xor_sync(0xffffffffu, mn[d], o);
+            const unsigned long long b = __shfl_xor_sync(0xffffffffu, mx[d], o);
+            mn[d] = a < mn[d] ? a : mn[d];
+            mx[d] = b > mx[d] ? b : mx[d];
         }
     // block reduction, then one atomic per bound per block (per-warp atomics on six words serialise)
-    __shared__ double s_mn[TB / 32][3], s_mx[TB / 32][3];
+    __shared__ unsigned long long s_mn[TB / 32][3], s_mx[TB / 32][3];
     const int warp = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0)
         for (int d = 0; d < 3; ++d) { s_mn[warp][d] = mn[d]; s_mx[warp][d] = mx[d]; }
     __syncthreads();
     if (threadIdx.x < 3) {
         const int d = threadIdx.x;
-        double a = s_mn[0][d], b = s_mx[0][d];
-        for (int w = 1; w < TB / 32; ++w) { a = fmin(a, s_mn[w][d]); b = fmax(b, s_mx[w][d]); }
-        atomicMin(&bbox[d], ord_key(a));
-        atomicMax(&bbox[3 + d], ord_key(b));
+        unsigned long long a = s_mn[0][d], b = s_mx[0][d];
+        for (int w = 1; w < TB / 32; ++w) {
+            a = s_mn[w][d] < a ? s_mn[w][d] : a;
+            b = s_mx[w][d] > b ? s_mx[w][d] : b;
+        }
+        atomicMin(&bbox[d], a);
+        atomicMax(&bbox[3 + d], b);
     }
     if (bad) atomicOr((unsigned int*)&info[INFO_ERR], NB_ERRBIT_NONFINITE);
 }
@@ -101,7 +112,14 @@ __global__ void k_box(const unsigned long long* bbox, int fixed, double fx, doub
         hi[d] = ord_val(bbox[3 + d]);
     }
     BoxDev b;
-    if (fixed) {
+    // no finite coordinate on some axis (every particle non-finite, already flagged): a unit box
+    // keeps the rest of the step well defined until the host reports the error
+    const bool finite = isfinite(lo[0]) && isfinite(lo[1]) && isfinite(lo[2]) && isfinite(hi[0]) &&
+                        isfinite(hi[1]) && isfinite(hi[2]) && lo[0] <= hi[0] && lo[1] <= hi[1] && lo[2] <= hi[2];
+    if (!finite) {
+        atomicOr((unsigned int*)&info[INFO_ERR], NB_ERRBIT_NONFINITE);
+        b.ox = 0.0; b.oy = 0.0; b.oz = 0.0; b.side = 1.0;
+    } else if (fixed) {
         b.ox = fx; b.oy = fy; b.oz = fz; b.side = fside;
         if (lo[0] < fx || lo[1] < fy || lo[2] < fz || hi[0] >= fx + fside || hi[1] >= fy + fside ||
             hi[2] >= fz + fside)
@@ -111,16 +129,23 @@ __global__ void k_box(const unsigned long long* bbox, int fixed, double fx, doub
         double side = 1.0;
         while (side < ext) side *= 2.0;
         while (side * 0.5 >= ext && ext > 0) side *= 0.5;
-        double o[3];
-        for (;;) {
+        double o[3] = {0.0, 0.0, 0.0};
+        // finite bounds fit after a few doublings; the limit (the whole double range) only guards
+        // the loop against a box that cannot be represented
+        bool ok = false;
+        for (int it = 0; it < 2200 && !ok && isfinite(side); ++it) {
             double half = side * 0.5;
-            bool ok = true;
+            ok = true;
             for (int d = 0; d < 3; ++d) {
                 o[d] = floor(lo[d] / half) * half;
                 ok = ok && (o[d] + side > hi[d]);
             }
-            if (ok) break;
-            side *= 2.0;
+            if (!ok) side *= 2.0;
+        }
+        if (!ok) {
+            atomicOr((unsigned int*)&info[INFO_ERR], NB_ERRBIT_RANGE);
+            o[0] = o[1] = o[2] = 0.0;
+            side = 1.0;
         }
         b.ox = o[0]; b.oy = o[1]; b.oz = o[2]; b.side = side;
     }
