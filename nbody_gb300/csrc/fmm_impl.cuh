@@ -709,7 +709,7 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
                 S p[TPL][4];
 #pragma unroll
                 for (int j = 0; j < TPL; ++j) { p[j][0] = 0; p[j][1] = 0; p[j][2] = 0; p[j][3] = 0; }
-#pragma unroll 2
+#pragma unroll (TPL == 2 ? 4 : 2)
                 for (int e = 0; e < nj; ++e) {
                     const S4 sj = gtile[e];
 #pragma unroll

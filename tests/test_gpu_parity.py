@@ -221,6 +221,13 @@ def test_errors_are_reported(nb):
         s = nb.CudaSimulation.from_arrays(np.array([[np.nan, 0, 0], [0, 0, 0]]), None, np.ones(2), fixed_box=0,
                                           precision=nb.PREC_MIXED)
         s.forces()
+    # an infinite coordinate stays out of the root box (which must still fit the finite ones) and is
+    # reported, in both state precisions
+    for bad, prec in ((np.inf, nb.PREC_MIXED), (-np.inf, nb.PREC_FP32)):
+        with pytest.raises(nb.NbodyError):
+            s = nb.CudaSimulation.from_arrays(np.array([[0.1, bad, 0.2], [0, 0, 0], [0.5, 0.5, 0.5]]), None,
+                                              np.ones(3), fixed_box=0, precision=prec)
+            s.forces()
 
 
 def test_trajectory_file_rows(nb, tmp_path):
