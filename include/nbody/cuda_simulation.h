@@ -191,6 +191,21 @@ public:
     }
     void closeTrajectory() { check(nbody_trajectory_close(_ctx), "nbody_trajectory_close"); }
 
+    /* adaptive global step, dt = clamp(eta * sqrt(length / max|a|), dtMin, dtMax) each step
+       (length <= 0: the softening); setFixedTimestep() returns to the constructor's dt */
+    void setAdaptiveTimestep(double eta, double length, double dtMin, double dtMax) {
+        check(nbody_set_timestep_control(_ctx, NBODY_DT_ADAPTIVE, eta, length, dtMin, dtMax),
+              "nbody_set_timestep_control");
+    }
+    void setFixedTimestep() {
+        check(nbody_set_timestep_control(_ctx, NBODY_DT_FIXED, 0.0, 0.0, 0.0, 0.0), "nbody_set_timestep_control");
+    }
+    double lastTimestep() const {
+        double dt = 0.0;
+        check(nbody_last_timestep(_ctx, &dt), "nbody_last_timestep");
+        return dt;
+    }
+
     nbody_ctx* handle() const { return _ctx; }
 };
 

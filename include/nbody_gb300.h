@@ -95,6 +95,27 @@ int nbody_get_state(nbody_ctx* c, int order, double* pos, double* vel, double* m
    time after the last step. */
 int nbody_step(nbody_ctx* c, int nsteps, double* t_out);
 
+/* Step-size control.  The reference integrates with one fixed dt and lists a
+   variable time step among its goals (TODO: "variable timestep"); this is a
+   global adaptive step on top of the fused integrator.
+   mode NBODY_DT_FIXED: every step takes params.dt (the default).
+   mode NBODY_DT_ADAPTIVE: each step takes
+       dt = clamp(eta * sqrt(length / max_i |a_i|), dt_min, dt_max)
+   from the accelerations of the last force evaluation: for the leapfrog
+   those at the start of the step (so each kick-drift-kick step uses one dt),
+   for explicit Euler those of the previous step.  length <= 0 takes the
+   softening eps (which must then be > 0).  max |a_i|^2 is reduced on the
+   device with the evaluation and read at the step's existing
+   synchronisation.  The recorded run of the adjoint
+   (nbody_forward_checkpointed) needs mode NBODY_DT_FIXED.  Returning to
+   NBODY_DT_FIXED restores the dt the context had before. */
+#define NBODY_DT_FIXED 0
+#define NBODY_DT_ADAPTIVE 1
+int nbody_set_timestep_control(nbody_ctx* c, int mode, double eta, double length, double dt_min, double dt_max);
+
+/* The dt of the last step taken (params.dt before any step). */
+int nbody_last_timestep(nbody_ctx* c, double* dt);
+
 /* Accelerations (n x 3) and, if pot != NULL, potential per unit charge (n) at
    the current positions, in input order, without advancing.  This is the
    force evaluation that the reference keeps private

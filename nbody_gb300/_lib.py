@@ -20,13 +20,15 @@ ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: 
 
 PREC_FP32, PREC_MIXED, PREC_FP64 = 0, 1, 2
 INTEG_LEAPFROG, INTEG_EULER = 0, 1
+DT_FIXED, DT_ADAPTIVE = 0, 1
 
 EXPORTS = ("nbody_default_params", "nbody_create", "nbody_destroy", "nbody_set_state", "nbody_get_state",
            "nbody_step", "nbody_compute_forces", "nbody_diagnostics", "nbody_tree_info", "nbody_get_tree",
            "nbody_get_interactions", "nbody_set_timing", "nbody_phase_times", "nbody_stream", "nbody_get_time",
            "nbody_last_error", "nbody_direct_forces", "nbody_get_stats", "nbody_flops_per_m2l", "nbody_flops_per_p2p",
            "nbody_measure_peaks", "nbody_direct_forces_static", "nbody_force_vjp", "nbody_forward_checkpointed",
-           "nbody_backward", "nbody_device_memory", "nbody_trajectory_open", "nbody_trajectory_close")
+           "nbody_backward", "nbody_device_memory", "nbody_trajectory_open", "nbody_trajectory_close",
+           "nbody_set_timestep_control", "nbody_last_timestep")
 
 
 class Params(C.Structure):
@@ -90,6 +92,8 @@ def load(path: str | None = None):
     L.nbody_stream.argtypes = [vp]
     L.nbody_stream.restype = vp
     L.nbody_get_time.argtypes = [vp, C.POINTER(C.c_double)]
+    L.nbody_set_timestep_control.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]
+    L.nbody_last_timestep.argtypes = [vp, C.POINTER(C.c_double)]
     L.nbody_last_error.argtypes = [vp]
     L.nbody_last_error.restype = C.c_char_p
     for name in EXPORTS:

@@ -249,6 +249,8 @@ int nbody_forward_checkpointed(nbody_ctx* c, int nsteps, int every, double* t_ou
     if (c->n == 0) return nb_fail(c, NBODY_ERR_STATE, "no particles");
     if (c->prm.integrator != NBODY_INTEG_LEAPFROG)
         return nb_fail(c, NBODY_ERR_INVALID, "the recorded run needs the leapfrog integrator");
+    if (c->dt_mode != NBODY_DT_FIXED)
+        return nb_fail(c, NBODY_ERR_STATE, "the recorded run differentiates fixed steps: switch adaptive steps off");
     if (nsteps < 1 || every < 0) return nb_fail(c, NBODY_ERR_INVALID, "nsteps must be >= 1 and every >= 0");
     NB_CU(c, cudaSetDevice(c->device));
     const bool rec = every == 0;

@@ -2,6 +2,7 @@
 // loop and inspection calls.  Declarations and reference citations are in
 // include/nbody_gb300.h.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -190,6 +191,46 @@ int fmm(nbody_ctx* c, int integ, bool want_pot) {
     }
 }
 
+// max_i |a_i|^2 of the current accelerations for the adaptive step: block maxima, then one atomicMax
+// per block on the bit pattern (non-negative doubles order like their bits; NaN never wins a compare)
+template <typename R>
+__global__ void __launch_bounds__(TB) k_amax2(int64_t n, const R* __restrict__ ax, const R* __restrict__ ay,
+                                               const R* __restrict__ az, unsigned long long* out) {
+    double m = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x; i < n; i += (int64_t)gridDim.x * TB) {
+        const double x = (double)ax[i], y = (double)ay[i], z = (double)az[i];
+        const double a2 = x * x + y * y + z * z;
+        m = a2 > m ? a2 : m;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double v = __shfl_xor_sync(0xffffffffu, m, o);
+        m = v > m ? v : m;
+    }
+    __shared__ double s_m[TB / 32];
+    if ((threadIdx.x & 31) == 0) s_m[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < TB / 32; ++w) m = s_m[w] > m ? s_m[w] : m;
+        atomicMax(out, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+// queues the reduction and the copy of its result to pinned memory (read after the next sync)
+template <typename R>
+int amax_t(nbody_ctx* c) {
+    const int k = c->cur;
+    unsigned g = std::min<unsigned>(nblk(c->n), 152 * 8);
+    if (g == 0) g = 1;
+    NB_CU(c, cudaMemsetAsync(c->amax.p, 0, sizeof(unsigned long long), c->st));
+    k_amax2<R><<<g, TB, 0, c->st>>>(c->n, DP<R>(c->ax[k]), DP<R>(c->ay[k]), DP<R>(c->az[k]),
+                                    DP<unsigned long long>(c->amax));
+    NB_LAUNCHED(c, "acceleration maximum");
+    c->launches += 1;
+    NB_CU(c, cudaMemcpyAsync(c->h_amax, c->amax.p, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    return NBODY_OK;
+}
+
 }  // namespace
 
 // one force evaluation at the current positions, with an optional integrator epilogue
@@ -204,6 +245,10 @@ int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
     if (c->timing) cudaEventRecord(c->ev[2], c->st);
     NB_TRY(nb_build_tree(c));
     NB_TRY(fmm(c, integ, want_pot));
+    // adaptive steps: the largest acceleration of this evaluation, read at the sync below
+    c->amax_valid = false;
+    const bool adaptive = c->dt_mode == NBODY_DT_ADAPTIVE;
+    if (adaptive) NB_TRY(c->rsz == 4 ? amax_t<float>(c) : amax_t<double>(c));
     // error bits raised after the traversal check (asynchronous copies of the far field)
     NB_CU(c, cudaMemcpyAsync(c->h_info, c->info.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->st));
     NB_CU(c, cudaStreamSynchronize(c->st));
@@ -213,8 +258,21 @@ int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
         NB_CU(c, cudaEventSynchronize(c->ev[7]));
         for (int i = 0; i < 7; ++i) cudaEventElapsedTime(&c->phase_ms[i], c->ev[i], c->ev[i + 1]);
     }
+    if (adaptive) {
+        c->amax2 = *c->h_amax;
+        c->amax_valid = true;
+    }
     c->eval_current = true;
     return NBODY_OK;
+}
+
+// the adaptive dt from the last evaluation's largest acceleration (nbody_set_timestep_control)
+static double adaptive_dt(const nbody_ctx* c) {
+    const double len = c->dt_len > 0.0 ? c->dt_len : c->prm.eps;
+    double dt = c->amax2 > 0.0 ? c->dt_eta * std::sqrt(len / std::sqrt(c->amax2)) : c->dt_max;
+    if (!(dt >= c->dt_min)) dt = c->dt_min;       // also a non-finite candidate
+    if (dt > c->dt_max) dt = c->dt_max;
+    return dt;
 }
 
 namespace {
@@ -325,6 +383,8 @@ int nbody_destroy(nbody_ctx* c) {
         release(*b);
     for (EvalRecord& r : c->recs) release(r.buf);
     if (c->h_info) cudaFreeHost(c->h_info);
+    if (c->h_amax) cudaFreeHost(c->h_amax);
+    release(c->amax);
     for (int i = 0; i < 16; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (int i = 0; i < NB_P2P_CLASSES; ++i) {
@@ -371,6 +431,7 @@ int nbody_set_state(nbody_ctx* c, int64_t n, const double* pos, const double* ve
     NB_CU(c, cudaStreamSynchronize(c->st));
     c->time = 0.0;
     c->have_acc = acc != nullptr;
+    c->amax_valid = false;
     c->ck_steps = 0;
     c->eval_current = false;
     return NBODY_OK;
@@ -405,6 +466,16 @@ int nbody_step(nbody_ctx* c, int nsteps, double* t_out) {
     NB_CU(c, cudaSetDevice(c->device));
     if (nsteps > 0) c->ck_steps = 0;
     for (int s = 0; s < nsteps; ++s) {
+        if (c->dt_mode == NBODY_DT_ADAPTIVE) {
+            // this step's dt needs the largest acceleration at the current positions (leapfrog) or
+            // of the last evaluation (Euler); without one, evaluate the forces first
+            if (!c->amax_valid) {
+                NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
+                c->have_acc = c->prm.integrator == NBODY_INTEG_LEAPFROG;
+            }
+            c->prm.dt = adaptive_dt(c);
+        }
+        c->dt_last = c->prm.dt;
         if (c->prm.integrator == NBODY_INTEG_LEAPFROG) {
             if (!c->have_acc) {
                 NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
@@ -545,6 +616,40 @@ int nbody_device_memory(nbody_ctx* c, int64_t* current, int64_t* peak) {
     if (!c) return NBODY_ERR_INVALID;
     if (current) *current = (int64_t)c->dev_bytes;
     if (peak) *peak = (int64_t)c->dev_peak;
+    return NBODY_OK;
+}
+
+int nbody_set_timestep_control(nbody_ctx* c, int mode, double eta, double length, double dt_min, double dt_max) {
+    if (!c) return NBODY_ERR_INVALID;
+    if (mode == NBODY_DT_FIXED) {
+        if (c->dt_mode == NBODY_DT_ADAPTIVE) c->prm.dt = c->dt_base;
+        c->dt_mode = NBODY_DT_FIXED;
+        c->amax_valid = false;
+        return NBODY_OK;
+    }
+    if (mode != NBODY_DT_ADAPTIVE) return nb_fail(c, NBODY_ERR_INVALID, "mode must be NBODY_DT_FIXED or NBODY_DT_ADAPTIVE");
+    if (!(eta > 0.0) || !std::isfinite(eta)) return nb_fail(c, NBODY_ERR_INVALID, "eta must be > 0");
+    if (!(dt_min > 0.0) || !(dt_max >= dt_min) || !std::isfinite(dt_max))
+        return nb_fail(c, NBODY_ERR_INVALID, "need 0 < dt_min <= dt_max < inf");
+    if (!(length > 0.0) && !(c->prm.eps > 0.0))
+        return nb_fail(c, NBODY_ERR_INVALID, "length must be > 0 when the softening eps is 0");
+    if (!std::isfinite(length)) return nb_fail(c, NBODY_ERR_INVALID, "length must be finite");
+    NB_CU(c, cudaSetDevice(c->device));
+    NB_TRY(nb_grow(c, c->amax, sizeof(unsigned long long)));
+    if (!c->h_amax) NB_CU(c, cudaMallocHost(&c->h_amax, sizeof(double)));
+    if (c->dt_mode == NBODY_DT_FIXED) c->dt_base = c->prm.dt;
+    c->dt_mode = NBODY_DT_ADAPTIVE;
+    c->dt_eta = eta;
+    c->dt_len = length;
+    c->dt_min = dt_min;
+    c->dt_max = dt_max;
+    c->amax_valid = false;
+    return NBODY_OK;
+}
+
+int nbody_last_timestep(nbody_ctx* c, double* dt) {
+    if (!c || !dt) return NBODY_ERR_INVALID;
+    *dt = c->dt_last > 0.0 ? c->dt_last : c->prm.dt;
     return NBODY_OK;
 }
 

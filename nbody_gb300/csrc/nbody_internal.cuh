@@ -166,6 +166,16 @@ struct nbody_ctx {
 
     nb_traj* traj = nullptr;       // open trajectory file, if any
 
+    // step-size control (nbody_set_timestep_control)
+    int dt_mode = NBODY_DT_FIXED;
+    double dt_eta = 0, dt_len = 0, dt_min = 0, dt_max = 0;
+    double dt_base = 0;            // params.dt before adaptive steps were switched on
+    double dt_last = 0;            // dt of the last step
+    bool amax_valid = false;       // amax2 holds max |a|^2 of the current accelerations
+    double amax2 = 0;
+    DevBuf amax;                   // device word of the reduction (bits of a non-negative double)
+    double* h_amax = nullptr;      // pinned copy
+
     std::string err;
 };
 

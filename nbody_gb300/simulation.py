@@ -236,6 +236,20 @@ class CudaSimulation:
     def trajectory_close(self):
         check(self._h, _lib.load().nbody_trajectory_close(self._h))
 
+    def set_timestep_control(self, mode: str = "adaptive", eta: float = 0.02, length: float = 0.0,
+                             dt_min: float = 1e-8, dt_max: float = 1e-2):
+        """Adaptive global step: dt = clamp(eta * sqrt(length / max|a|), dt_min, dt_max) from the last
+        evaluation's accelerations (length <= 0: the softening eps); mode "fixed" restores params.dt."""
+        m = {"fixed": _lib.DT_FIXED, "adaptive": _lib.DT_ADAPTIVE}[mode]
+        check(self._h, _lib.load().nbody_set_timestep_control(self._h, m, float(eta), float(length), float(dt_min),
+                                                              float(dt_max)))
+
+    def last_timestep(self) -> float:
+        """dt of the last step taken."""
+        dt = C.c_double()
+        check(self._h, _lib.load().nbody_last_timestep(self._h, C.byref(dt)))
+        return dt.value
+
     def device_memory(self):
         """(bytes held on the device now, high-water mark since creation)."""
         cur, peak = C.c_int64(), C.c_int64()

@@ -241,6 +241,36 @@ def leapfrog(pos, vel, q, m, eps, G, dt, steps, nthreads=None):
     return pos.reshape(-1, 3), vel.reshape(-1, 3), acc.reshape(-1, 3)
 
 
+def adaptive_dt(acc, eta, length, dt_min, dt_max):
+    """The adaptive step rule of nbody_set_timestep_control: clamp(eta * sqrt(length / max|a|), dt_min,
+    dt_max), with max|a|^2 summed per particle as x*x + y*y + z*z.  The reference only lists a variable
+    time step as a goal (its TODO file), so this restates the library's own rule."""
+    acc = np.asarray(acc, dtype=np.float64).reshape(-1, 3)
+    a2 = float(np.max(acc[:, 0] * acc[:, 0] + acc[:, 1] * acc[:, 1] + acc[:, 2] * acc[:, 2])) if len(acc) else 0.0
+    dt = eta * np.sqrt(length / np.sqrt(a2)) if a2 > 0.0 else dt_max
+    if not dt >= dt_min:
+        dt = dt_min
+    return min(dt, dt_max)
+
+
+def leapfrog_adaptive(pos, vel, q, m, eps, G, eta, length, dt_min, dt_max, steps, nthreads=None):
+    """FP64 direct-sum kick-drift-kick leapfrog whose step n takes adaptive_dt of the accelerations at
+    its start (length <= 0: eps); returns (pos, vel, acc, dts)."""
+    pos = np.array(pos, dtype=np.float64).reshape(-1, 3)
+    vel = np.array(vel, dtype=np.float64).reshape(-1, 3)
+    length = length if length > 0.0 else eps
+    acc = direct(pos, q, m, eps, G, nthreads=nthreads)[0]
+    dts = []
+    for _ in range(steps):
+        dt = adaptive_dt(acc, eta, length, dt_min, dt_max)
+        vel = vel + (0.5 * dt) * acc
+        pos = pos + dt * vel
+        acc = direct(pos, q, m, eps, G, nthreads=nthreads)[0]
+        vel = vel + (0.5 * dt) * acc
+        dts.append(dt)
+    return pos, vel, acc, np.array(dts)
+
+
 def direct_vjp(pos, q, m, mu, eps=0.01, G=1.0, nthreads=None):
     """FP64 direct-sum VJP of S = sum_i mu_i . a_i: (dS/dx, dS/dq, dS/dm)."""
     pos = np.ascontiguousarray(pos, np.float64).reshape(-1)

@@ -296,3 +296,24 @@ def test_frozen_tree_fmm_derivative_approaches_direct_vjp(oracle):
     t.set_particles(pos=pos)
     assert errs[0] > errs[1] > errs[2]
     assert errs[2] < 1e-5 and errs[0] < 2e-2
+
+
+def test_adaptive_leapfrog_with_a_pinned_step_is_the_fixed_leapfrog(oracle):
+    """dt_min = dt_max pins the adaptive rule to one step: the adaptive restatement then walks the
+    same trajectory as the C leapfrog."""
+    rng = np.random.default_rng(61)
+    pos, vel = rng.normal(size=(200, 3)), 0.1 * rng.normal(size=(200, 3))
+    m = np.full(200, 1.0 / 200)
+    p1, v1, _, dts = oracle.leapfrog_adaptive(pos, vel, m, m, 0.05, 1.0, 0.1, 0.0, 1e-3, 1e-3, 5)
+    p2, v2, _ = oracle.leapfrog(pos, vel, m, m, 0.05, 1.0, 1e-3, 5)
+    assert np.all(dts == 1e-3)
+    np.testing.assert_allclose(p1, p2, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(v1, v2, rtol=0, atol=1e-12)
+
+
+def test_adaptive_dt_rule(oracle):
+    acc = np.array([[3.0, 4.0, 0.0], [0.0, 0.0, 1.0]])          # max |a| = 5
+    assert oracle.adaptive_dt(acc, 0.1, 0.05, 1e-6, 1.0) == pytest.approx(0.1 * np.sqrt(0.05 / 5.0), rel=1e-15)
+    assert oracle.adaptive_dt(acc, 0.1, 0.05, 1e-6, 1e-3) == 1e-3       # clamped above
+    assert oracle.adaptive_dt(acc, 1e-9, 0.05, 1e-6, 1.0) == 1e-6       # clamped below
+    assert oracle.adaptive_dt(np.zeros((4, 3)), 0.1, 0.05, 1e-6, 0.5) == 0.5   # no acceleration: dt_max
