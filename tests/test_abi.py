@@ -70,3 +70,49 @@ def test_create_without_a_device_fails_cleanly(nb):
     assert b"device" in L.nbody_last_error(None)
     with pytest.raises(nb.NbodyError):
         nb.CudaSimulation([1.0, 1.0, 1.0], [], 1e-3)
+
+
+def test_null_context_is_refused_by_every_entry_point(nb):
+    """Every call that takes a context returns NBODY_ERR_INVALID for NULL (no crash, no device)."""
+    from nbody_gb300 import _lib
+    L = _lib.load()
+    d = C.c_double()
+    i64 = C.c_int64()
+    calls = {
+        "nbody_set_state": (None, 0, None, None, None, None, None),
+        "nbody_get_state": (None, 0, None, None, None, None, None, None),
+        "nbody_step": (None, 1, C.byref(d)),
+        "nbody_compute_forces": (None, None, None),
+        "nbody_diagnostics": (None, None),
+        "nbody_tree_info": (None, None, None, None, None),
+        "nbody_get_tree": (None, None, None, None),
+        "nbody_get_interactions": (None, 0, C.byref(i64), None),
+        "nbody_set_timing": (None, 1),
+        "nbody_get_time": (None, C.byref(d)),
+        "nbody_device_memory": (None, None, None),
+        "nbody_force_vjp": (None, None, None, None, None),
+        "nbody_forward_checkpointed": (None, 1, 0, C.byref(d)),
+        "nbody_backward": (None, None, None, None, None, None, None),
+        "nbody_trajectory_open": (None, b"x.csv", 1, 0, 6),
+        "nbody_trajectory_close": (None,),
+        "nbody_set_timestep_control": (None, 1, 0.02, 0.0, 1e-6, 1e-2),
+        "nbody_last_timestep": (None, C.byref(d)),
+    }
+    for name, args in calls.items():
+        assert getattr(L, name)(*args) == 1, name
+    assert L.nbody_stream(None) is None
+    assert L.nbody_destroy(None) == 0
+
+
+@pytest.mark.parametrize("src", ["drop_in_main.cpp", "adjoint_main.cpp"])
+def test_cpp_drop_in_programs_compile_against_the_headers(src):
+    """The C++ drop-in (include/nbody/cuda_simulation.h over the C ABI) compiles as the reference's
+    C++14 code would use it, warnings as errors; linking and running need the GPU tests."""
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    r = subprocess.run(["g++", "-std=c++14", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only",
+                        "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
