@@ -342,8 +342,8 @@ def main():
                   "phase": "near field + L2P + integrator: six leaf-size class kernels side by side + split-leaf sums",
                   "traffic_bytes": 261.9e6 if default_cfg else None},
         "k_m2l": {"ms": per_step[5], "tflops": m2l_tf, "flops_per_launch": m2l_flops, "launches": 1,
-                  "phase": "M2L (+ depth L2L launches, 11 % of the phase)",
-                  "traffic_bytes": 265.5e6 if default_cfg else None},
+                  "phase": "M2L (+ depth L2L launches, ~6 % of the phase)",
+                  "traffic_bytes": 265.4e6 if default_cfg else None},
     }
     dom = "k_m2l" if per_step[5] >= per_step[6] else "k_p2p"
     ach = kernels[dom]["tflops"]
