@@ -167,7 +167,7 @@ inline size_t al256(size_t b) { return (b + 255) / 256 * 256; }
 int rec_save(nbody_ctx* c, int j) {
     if ((int)c->recs.size() <= j) c->recs.resize(j + 1);
     EvalRecord& R = c->recs[j];
-    RecField f[24];
+    RecField f[24] = {};
     const int nf = rec_fields(c, c->nnodes, c->nleaves, (uint32_t)c->h_info[INFO_M2L_TAIL],
                               (uint32_t)c->h_info[INFO_P2P_TAIL], f);
     size_t total = 0;
@@ -191,7 +191,7 @@ int rec_save(nbody_ctx* c, int j) {
 // sorted charges, masses, accelerations and ids; positions and velocities are left alone)
 int rec_load(nbody_ctx* c, int j) {
     EvalRecord& R = c->recs[j];
-    RecField f[24];
+    RecField f[24] = {};
     const int nf = rec_fields(c, R.nn, R.nl, (uint32_t)R.info[INFO_M2L_TAIL], (uint32_t)R.info[INFO_P2P_TAIL], f);
     size_t o = 0;
     for (int i = 0; i < nf; ++i) {
