@@ -187,9 +187,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-targets", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--adj-steps", type=int, default=10, help="steps of the timed forward+adjoint run (0: skip)")
-    ap.add_argument("--adj-every", type=int, default=0,
-                    help="checkpoint spacing of the forward+adjoint run (0: every evaluation recorded)")
+    ap.add_argument("--adj-steps", type=int, default=20, help="steps of the timed forward+adjoint runs (0: skip)")
+    ap.add_argument("--adj-every", type=int, default=20,
+                    help="checkpoint spacing of the headline forward+adjoint run (recomputation inside each "
+                         "segment); a second run keeps every evaluation (spacing 0)")
+    ap.add_argument("--fp64-caps", default="64,32",
+                    help="leaf capacities tried for the plain FP64 GPU FMM at the same order ('' to skip)")
+    ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of each FP64 configuration")
+    ap.add_argument("--drift-steps", type=int, default=1000,
+                    help="leapfrog steps of the energy / momentum drift run from the initial state (0: skip)")
     a = ap.parse_args()
     assert a.warmup >= 0 and a.steps >= 1
     rank, world, local = dist_env()
@@ -274,8 +280,10 @@ def main():
     e2e = a.n * a.e2e_steps * world / e2e_s
 
     # forward + adjoint: a recorded run of adj_steps steps and its reverse sweep, with the loss
-    # L = sum(wx . x_N + wv . v_N); seeds and gradients stay on the device
+    # L = sum(wx . x_N + wv . v_N); seeds and gradients stay on the device.  Headline: checkpoints
+    # every adj_every steps with recomputation inside each segment; beside it every evaluation kept.
     fwd_adj = None
+    fwd_adj_rec = None
     if a.adj_steps > 0:
         dev = torch.device("cuda", local)
         g = torch.Generator(device=dev).manual_seed(7)
@@ -286,25 +294,39 @@ def main():
         dp = lambda t: ctypes.c_void_p(t.data_ptr())
         L = _lib.load()
 
-        def fwd_bwd(k):
-            _lib.check(sim._h, L.nbody_forward_checkpointed(sim._h, k, a.adj_every, None))
+        def fwd_bwd(k, every):
+            _lib.check(sim._h, L.nbody_forward_checkpointed(sim._h, k, every, None))
             _lib.check(sim._h, L.nbody_backward(sim._h, dp(wx), dp(wv), *(dp(t) for t in out)))
 
-        fwd_bwd(min(2, a.adj_steps))           # warm-up: snapshot and adjoint buffers
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-        ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        ea.record(stream)
-        fwd_bwd(a.adj_steps)
-        eb.record(stream)
-        torch.cuda.synchronize()
-        adj_ms = ea.elapsed_time(eb)
-        if world > 1:
-            t = torch.tensor([adj_ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            adj_ms = float(t.item())
+        def timed_fwd_bwd(every):
+            fwd_bwd(min(2, a.adj_steps), every)           # warm-up: snapshot and adjoint buffers
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ea.record(stream)
+            fwd_bwd(a.adj_steps, every)
+            eb.record(stream)
+            torch.cuda.synchronize()
+            t_ms = ea.elapsed_time(eb)
+            if world > 1:
+                t = torch.tensor([t_ms], device="cuda")
+                torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+                t_ms = float(t.item())
+            return t_ms
+
+        fwd_ms = ms / a.steps
+        rec_ms = timed_fwd_bwd(0)
+        fin_rec = all(bool(torch.isfinite(t).all()) for t in out)
+        rec_peak = sim.device_memory()[1]
+        adj_ms = timed_fwd_bwd(a.adj_every)
         fin = all(bool(torch.isfinite(t).all()) for t in out)
+        fwd_adj_rec = {"value": a.n * a.adj_steps * world / (rec_ms * 1e-3), "unit": UNIT,
+                       "ms_per_step": rec_ms / a.adj_steps, "steps": a.adj_steps, "checkpoint_every": 0,
+                       "cost_vs_forward_step": rec_ms / a.adj_steps / fwd_ms, "gradients_finite": fin_rec,
+                       "device_peak_bytes": rec_peak,
+                       "note": "every evaluation kept whole (tree, lists, local expansions): the reverse sweep "
+                               "re-evaluates nothing"}
         # phases of one force VJP at the final state
         sim.set_timing(True)
         mu = (wv * a.dt).cpu().numpy()
@@ -314,11 +336,76 @@ def main():
         sim.set_timing(False)
         fwd_adj = {"value": a.n * a.adj_steps * world / (adj_ms * 1e-3), "unit": UNIT,
                    "ms_per_step": adj_ms / a.adj_steps, "steps": a.adj_steps, "checkpoint_every": a.adj_every,
+                   "cost_vs_forward_step": adj_ms / a.adj_steps / fwd_ms,
                    "gradients_finite": fin, "vjp_phase_ms": vjp_ph, "vjp_launches": vjp_launches,
-                   "note": "one recorded leapfrog run of `steps` steps plus its reverse sweep (frozen-tree "
-                           "discrete adjoint: one force VJP per time point, re-evaluation from snapshots); "
+                   "recorded_every_evaluation": fwd_adj_rec,
+                   "note": "one leapfrog run of `steps` steps with a sorted-state checkpoint every "
+                           "`checkpoint_every` steps, plus its reverse sweep (frozen-tree discrete adjoint: "
+                           "each segment recomputed forward from its checkpoint, one force VJP per time point); "
+                           "cost_vs_forward_step = (forward + adjoint ms per step) / forward ms per step; "
                            "loss sum(wx . x_N + wv . v_N), seeds and gradients resident on the device"}
         del out, wx, wv
+
+    # spec: the plain FP64 GPU FMM at equal accuracy, on the same initial conditions and time
+    # point (warm-up steps), the same order, for each leaf capacity tried; the fastest whose rms error
+    # is within 5 % of the mixed form's (or at most 1e-4) is the comparator
+    fp64_cmp = None
+    caps = [int(x) for x in a.fp64_caps.split(",") if x.strip()] if a.precision == "mixed" else []
+    if caps:
+        tried = []
+        for cap in caps:
+            s64 = nb.CudaSimulation.from_arrays(pos, vel, m, m, precision=nb.PREC_FP64, order=a.order,
+                                                leaf_capacity=cap, theta=a.theta, eps=a.eps, dt=a.dt,
+                                                integrator=nb.INTEG_LEAPFROG, fixed_box=0, device=local)
+            st64 = torch.cuda.ExternalStream(s64.stream, device=torch.device("cuda", local))
+            for _ in range(a.warmup):
+                s64.step(1)
+            a64 = s64.forces()
+            d64, _ = s64.direct(tg)
+            e64 = np.linalg.norm(a64[tg] - d64, axis=1) / np.linalg.norm(d64, axis=1)
+            rms64 = float(np.sqrt(np.mean(e64 ** 2)))
+            s64.step(1)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st64)
+            s64.step(a.fp64_steps)
+            e1.record(st64)
+            torch.cuda.synchronize()
+            ms64 = e0.elapsed_time(e1) / a.fp64_steps
+            tried.append({"leaf_capacity": cap, "order": a.order, "ms_per_step": ms64,
+                          "value": a.n / (ms64 * 1e-3), "rms_err": rms64})
+            s64.close()
+        ok = [t for t in tried if t["rms_err"] <= max(1.05 * rms_err, 1e-4)]
+        best = min(ok or tried, key=lambda t: t["ms_per_step"])
+        fp64_cmp = {"unit": UNIT, "best": best, "tried": tried, "mixed_rms_err": rms_err,
+                    "speedup_mixed_over_fp64": value / world / best["value"],
+                    "target": ">= 2x at equal rms force error (<= 1e-4 vs FP64 direct sum)",
+                    "note": "plain FP64 GPU FMM (every stage in FP64) on the same ICs and time point; error on "
+                            "the same targets vs the FP64 direct sum; timed steps on its own stream"}
+
+    # config 2 as specified: 1,000 leapfrog steps of the collision from its initial state, FP64
+    # energy and momentum drift from nbody_diagnostics
+    drift = None
+    if a.drift_steps > 0:
+        sd = nb.CudaSimulation.from_arrays(pos, vel, m, m, precision=prec, order=a.order, leaf_capacity=a.cap,
+                                           theta=a.theta, eps=a.eps, dt=a.dt, integrator=nb.INTEG_LEAPFROG,
+                                           fixed_box=0, device=local)
+        d0 = sd.diagnostics()
+        w0 = time.perf_counter()
+        sd.step(a.drift_steps)
+        wd = time.perf_counter() - w0
+        d1 = sd.diagnostics()
+        e_0 = d0["kinetic"] + d0["potential"]
+        e_1 = d1["kinetic"] + d1["potential"]
+        drift = {"steps": a.drift_steps, "t_end": a.drift_steps * a.dt, "energy_0": e_0, "energy_end": e_1,
+                 "rel_energy_drift": (e_1 - e_0) / abs(e_0),
+                 "momentum_drift": float(np.abs(np.asarray(d1["momentum"]) - np.asarray(d0["momentum"])).max()),
+                 "angular_momentum_drift": float(np.abs(np.asarray(d1["angular_momentum"]) -
+                                                        np.asarray(d0["angular_momentum"])).max()),
+                 "wall_s": wd, "particle_steps_per_s_wall": a.n * a.drift_steps / wd,
+                 "note": "FP64 sums of the state and of the FMM potential (same form, order, capacity as the "
+                         "timed run); total mass 1"}
+        sd.close()
 
     if rank != 0:
         if world > 1:
@@ -363,7 +450,8 @@ def main():
         "dtype": "f32+f64" if a.precision == "mixed" else ("f32" if a.precision == "fp32" else "f64"),
         "data": f"synthetic seeded collision ICs (seed {a.seed} + rank)", "config": workload_desc(a),
         "rms_force_err_vs_fp64_direct": rms_err, "max_force_err_vs_fp64_direct": max_err,
-        "err_targets": int(len(tg)), "fwd_adjoint": fwd_adj,
+        "err_targets": int(len(tg)), "fwd_adjoint": fwd_adj, "fp64_equal_error": fp64_cmp,
+        "energy_momentum_drift": drift,
         "phase_ms_per_step": {k: float(v) for k, v in zip(nb.CudaSimulation.PHASES, per_step)},
         "work_per_step": stats, "wall_s_timed": wall,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": a.n * 8 * 11, "d2h_bytes_per_step": a.n * 8 * 9,

@@ -125,7 +125,7 @@ public:
     CudaSimulation(CudaSimulation const&) = delete;
     CudaSimulation& operator=(CudaSimulation const&) = delete;
 
-    ~CudaSimulation() override { nbody_destroy(_ctx); }
+    ~CudaSimulation() { nbody_destroy(_ctx); }
 
     Scalar step() override {
         double t = 0.0;
@@ -204,6 +204,16 @@ public:
         double dt = 0.0;
         check(nbody_last_timestep(_ctx, &dt), "nbody_last_timestep");
         return dt;
+    }
+
+    /* particles leaving the fixed root box [0, bounds): NBODY_ESCAPE_GROW (default) steps on the
+       smallest grown box that keeps [0, bounds) as one of its cells, NBODY_ESCAPE_ERROR makes
+       step() throw; grownBoxes() counts the evaluations that took a grown box */
+    void setEscapePolicy(int policy) { check(nbody_set_escape_policy(_ctx, policy), "nbody_set_escape_policy"); }
+    int64_t grownBoxes() const {
+        int64_t s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        check(nbody_get_stats(_ctx, s, 8), "nbody_get_stats");
+        return s[7];
     }
 
     nbody_ctx* handle() const { return _ctx; }

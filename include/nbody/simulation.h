@@ -30,7 +30,6 @@ public:
             : position(position), velocity(velocity), mass(mass), charge(charge) {}
     };
 
-    virtual ~Simulation() = default;
     /* advances one time step and returns the new time */
     virtual Scalar step() = 0;
     /* the particles, in the simulation's internal (octree leaf) order */

@@ -34,6 +34,8 @@ extern "C" {
 #define NBODY_ERR_CAPACITY 4     /* a bounded device structure overflowed */
 #define NBODY_ERR_STATE 5        /* call not valid in the current state */
 #define NBODY_ERR_NO_DEVICE 6    /* no CUDA device */
+#define NBODY_ERR_RANGE 7        /* a particle left the fixed root box (policy NBODY_ESCAPE_ERROR), or no
+                                    representable root box covers the particles */
 
 /* precision forms */
 #define NBODY_PREC_FP32 0        /* state and arithmetic in FP32 */
@@ -112,6 +114,25 @@ int nbody_step(nbody_ctx* c, int nsteps, double* t_out);
 #define NBODY_DT_FIXED 0
 #define NBODY_DT_ADAPTIVE 1
 int nbody_set_timestep_control(nbody_ctx* c, int mode, double eta, double length, double dt_min, double dt_max);
+
+/* Particles that leave a fixed root box (params.fixed_box = 1).  The
+   reference builds its octree over [0, bounds) (src/open_cl_simulation.cpp:
+   20,43-47) and re-inserts moved particles with the external octree's move()
+   (:120-123), whose handling of a particle outside the bounds is not part of
+   the reference.  Here:
+   NBODY_ESCAPE_GROW (the default): an evaluation whose particles do not all
+     lie in the box takes the smallest box of side box_size * 2^j that has
+     the fixed box as one of its level-j cells and covers every particle (so
+     particles inside the fixed box keep their cells below level j); the
+     count of such evaluations since nbody_set_state is nbody_get_stats
+     entry 7;
+   NBODY_ESCAPE_ERROR: such an evaluation fails with NBODY_ERR_RANGE before
+     any force is computed (with the leapfrog the opening kick and drift of
+     that step have already been applied; with explicit Euler the state is
+     the one before the step). */
+#define NBODY_ESCAPE_GROW 0
+#define NBODY_ESCAPE_ERROR 1
+int nbody_set_escape_policy(nbody_ctx* c, int policy);
 
 /* The dt of the last step taken (params.dt before any step). */
 int nbody_last_timestep(nbody_ctx* c, double* dt);
@@ -194,9 +215,11 @@ int nbody_direct_forces(nbody_ctx* c, int64_t nt, const int64_t* targets, double
    to 131072 per call (larger requests fail with NBODY_ERR_INVALID).  Every
    call on a device shares that array: calls that overlap on the GPU race and
    must be ordered by the caller.  The first call on a device looks up the
-   array's device address; make it before any stream capture on that device.
-   Target indices outside [0, n) give NaN results.  Errors:
-   nbody_last_error(NULL). */
+   array's device address; make it before any stream capture on that device
+   (after a cudaDeviceReset the next call looks it up again).  The call makes
+   `device` current for its launches and restores the calling thread's
+   previous current device before it returns.  Target indices outside
+   [0, n) give NaN results.  Errors: nbody_last_error(NULL). */
 int nbody_direct_forces_static(int device, int64_t n, const double* pos, const double* mass, const double* charge,
                                double eps, double G, int64_t nt, const int64_t* targets, double* acc, double* pot,
                                void* stream);
@@ -204,7 +227,9 @@ int nbody_direct_forces_static(int device, int64_t n, const double* pos, const d
 /* Work counters of the last force evaluation: out[0] far-field (M2L)
    cell pairs, out[1] near-field particle pairs, out[2] near-field leaf
    pairs, out[3] nodes, out[4] leaves, out[5] depth, out[6] kernel launches
-   of the last step.  n = number of entries wanted (<= 7). */
+   of the last step, out[7] evaluations since nbody_set_state whose fixed
+   root box was grown (nbody_set_escape_policy).  n = number of entries
+   wanted (<= 8). */
 int nbody_get_stats(nbody_ctx* c, int64_t* out, int n);
 
 /* Floating-point operations this build counts per far-field cell pair
@@ -250,6 +275,29 @@ void* nbody_stream(nbody_ctx* c);
 /* Device memory held by the context (its grow-only work buffers, snapshots and
    records) and its high-water mark since nbody_create, in bytes. */
 int nbody_device_memory(nbody_ctx* c, int64_t* current, int64_t* peak);
+
+/* Time limits of the device-side waits.  Every wait in a kernel of this
+   library is bounded; one that runs out raises an error word and the kernel
+   returns (it never traps or hangs), and the host turns the word into
+   NBODY_ERR_CUDA at its next synchronisation.  scan_polls bounds the polls of
+   one status word in the single-pass scans' look-back (default about a
+   second's worth); copy_cycles bounds, in SM clock cycles, the far-field
+   kernel's wait for its own bulk copies (default 2e9, about a second).  A
+   value <= 0 restores the default.  A scan that gives up leaves the context
+   failed for good (its state may be inconsistent): create a new one.  A
+   far-field wait that gives up fails that evaluation only. */
+int nbody_set_wait_limits(nbody_ctx* c, int64_t scan_polls, int64_t copy_cycles);
+
+/* Runs one of the bounded device waits on something that never completes and
+   reports it the way a step does, so the give-up path can be checked on a
+   GPU without a fault or a hang (no counterpart in the reference):
+   which = 0: the scans' look-back wait on a tile status word that nothing
+     publishes (context's scan_polls limit): NBODY_ERR_CUDA "a device scan did
+     not complete in time", which leaves the context failed like a real one;
+   which = 1: the far-field kernel's wait on an mbarrier that expects bytes no
+     copy delivers (context's copy_cycles limit): NBODY_ERR_CUDA "a far-field
+     copy did not complete in time"; the context stays usable. */
+int nbody_selftest_wait(nbody_ctx* c, int which);
 
 /* Simulated time. */
 int nbody_get_time(nbody_ctx* c, double* t);

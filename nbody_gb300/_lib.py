@@ -16,11 +16,12 @@ LIB_PATH = os.path.join(HERE, "libnbody_gb300.so")
 
 NBODY_OK = 0
 ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "capacity exceeded",
-          5: "invalid state", 6: "no CUDA device"}
+          5: "invalid state", 6: "no CUDA device", 7: "particle outside the root box"}
 
 PREC_FP32, PREC_MIXED, PREC_FP64 = 0, 1, 2
 INTEG_LEAPFROG, INTEG_EULER = 0, 1
 DT_FIXED, DT_ADAPTIVE = 0, 1
+ESCAPE_GROW, ESCAPE_ERROR = 0, 1
 
 EXPORTS = ("nbody_default_params", "nbody_create", "nbody_destroy", "nbody_set_state", "nbody_get_state",
            "nbody_step", "nbody_compute_forces", "nbody_diagnostics", "nbody_tree_info", "nbody_get_tree",
@@ -28,7 +29,8 @@ EXPORTS = ("nbody_default_params", "nbody_create", "nbody_destroy", "nbody_set_s
            "nbody_last_error", "nbody_direct_forces", "nbody_get_stats", "nbody_flops_per_m2l", "nbody_flops_per_p2p",
            "nbody_measure_peaks", "nbody_direct_forces_static", "nbody_force_vjp", "nbody_forward_checkpointed",
            "nbody_backward", "nbody_device_memory", "nbody_trajectory_open", "nbody_trajectory_close",
-           "nbody_set_timestep_control", "nbody_last_timestep")
+           "nbody_set_timestep_control", "nbody_last_timestep", "nbody_set_escape_policy", "nbody_set_wait_limits",
+           "nbody_selftest_wait")
 
 
 class Params(C.Structure):
@@ -94,6 +96,9 @@ def load(path: str | None = None):
     L.nbody_get_time.argtypes = [vp, C.POINTER(C.c_double)]
     L.nbody_set_timestep_control.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]
     L.nbody_last_timestep.argtypes = [vp, C.POINTER(C.c_double)]
+    L.nbody_set_escape_policy.argtypes = [vp, C.c_int]
+    L.nbody_set_wait_limits.argtypes = [vp, C.c_int64, C.c_int64]
+    L.nbody_selftest_wait.argtypes = [vp, C.c_int]
     L.nbody_last_error.argtypes = [vp]
     L.nbody_last_error.restype = C.c_char_p
     for name in EXPORTS:

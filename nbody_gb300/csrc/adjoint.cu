@@ -77,6 +77,7 @@ int snap_load(nbody_ctx* c, int slot) {
     NB_CU(c, cudaMemcpyAsync(id->p, base + 11 * rb, sizeof(uint32_t) * c->n, cudaMemcpyDeviceToDevice, c->st));
     c->have_acc = true;
     c->eval_current = false;
+    c->amax_valid = false;     // the adaptive step's max |a| belonged to the state before the load
     return NBODY_OK;
 }
 

@@ -490,6 +490,7 @@ int force_vjp(nbody_ctx* c, double coef) {
         B.eps2 = c->prm.eps * c->prm.eps;
         B.nnodes = nn;
         B.info = DP<int32_t>(c->info);
+        B.wait_cycles = c->copy_cycles;
         constexpr int W = M2LSmem<MODE, P>::warps;
         const size_t smem = (size_t)W * M2LSmem<MODE, P>::per_warp;
         NB_CU(c, cudaFuncSetAttribute(k_m2l<MODE, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -27,6 +28,9 @@ int nb_cuda(nbody_ctx* c, cudaError_t e, const char* what) {
 int nb_grow(nbody_ctx* c, DevBuf& b, size_t bytes) {
     if (bytes == 0) bytes = 16;
     if (b.bytes >= bytes) return NBODY_OK;
+    // allocation-failure injection for the error paths (NBODY_FAIL_ALLOC_AFTER at nbody_create)
+    if (c->alloc_fail_after >= 0 && c->alloc_calls++ >= c->alloc_fail_after)
+        return nb_fail(c, NBODY_ERR_NOMEM, "cudaMalloc: allocation failure injected by NBODY_FAIL_ALLOC_AFTER");
     if (b.p) {
         NB_CU(c, cudaStreamSynchronize(c->st));
         NB_CU(c, cudaFree(b.p));
@@ -233,6 +237,12 @@ int amax_t(nbody_ctx* c) {
 
 }  // namespace
 
+int nb_check_async(nbody_ctx* c) {
+    if ((uint32_t)c->h_info[INFO_ERR] & NB_ERRBIT_ASYNC)
+        return nb_fail(c, NBODY_ERR_CUDA, "a far-field copy did not complete in time");
+    return NBODY_OK;
+}
+
 // one force evaluation at the current positions, with an optional integrator epilogue
 int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
     c->launches = 0;
@@ -252,8 +262,7 @@ int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
     // error bits raised after the traversal check (asynchronous copies of the far field)
     NB_CU(c, cudaMemcpyAsync(c->h_info, c->info.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->st));
     NB_CU(c, cudaStreamSynchronize(c->st));
-    if ((uint32_t)c->h_info[INFO_ERR] & NB_ERRBIT_ASYNC)
-        return nb_fail(c, NBODY_ERR_CUDA, "a far-field copy did not complete in time");
+    NB_TRY(nb_check_async(c));
     if (c->timing) {
         NB_CU(c, cudaEventSynchronize(c->ev[7]));
         for (int i = 0; i < 7; ++i) cudaEventElapsedTime(&c->phase_ms[i], c->ev[i], c->ev[i + 1]);
@@ -336,6 +345,11 @@ int nbody_create(const nbody_params* p, nbody_ctx** out) {
     if (!c) return nb_fail(nullptr, NBODY_ERR_NOMEM, "host allocation failed");
     c->prm = *p;
     c->device = p->device;
+    if (const char* f = std::getenv("NBODY_FAIL_ALLOC_AFTER")) {
+        char* end = nullptr;
+        const long long k = std::strtoll(f, &end, 10);
+        if (end != f && k >= 0) c->alloc_fail_after = k;
+    }
     c->rsz = p->precision == NBODY_PREC_FP32 ? 4 : 8;
     int rc = NBODY_OK;
     do {
@@ -379,7 +393,7 @@ int nbody_destroy(nbody_ctx* c) {
                       &c->adj_gq, &c->adj_gm, &c->adj_nu, &c->adj_lamL, &c->adj_lamM, &c->adj_near,
                       &c->snaps, &c->lst_seg, &c->lst_nch, &c->lst_first, &c->lst_target, &c->lst_cnt,
                       &c->lst_off, &c->lst_cp, &c->lst_rows, &c->cls_key[0], &c->cls_key[1], &c->cls_val[0], &c->cls_val[1],
-                      &c->leaves_tmp})
+                      &c->leaves_tmp, &c->wait_probe})
         release(*b);
     for (EvalRecord& r : c->recs) release(r.buf);
     if (c->h_info) cudaFreeHost(c->h_info);
@@ -404,7 +418,11 @@ int nbody_set_state(nbody_ctx* c, int64_t n, const double* pos, const double* ve
     if (!pos || !mass) return nb_fail(c, NBODY_ERR_INVALID, "pos and mass are required");
     NB_CU(c, cudaSetDevice(c->device));
     NB_TRY(nb_traj_close(c));   // a trajectory file holds one particle set
-    c->n = n;
+    // no particles until the upload below has succeeded: a failed allocation leaves the context
+    // without state, so later calls fail with NBODY_ERR_STATE instead of reading missing buffers
+    c->n = 0;
+    c->ck_steps = 0;
+    c->eval_current = false;
     c->cur = 0;
     NB_TRY(alloc_state(c, n));
     double* st = DP<double>(c->stage);
@@ -429,6 +447,8 @@ int nbody_set_state(nbody_ctx* c, int64_t n, const double* pos, const double* ve
                                                     DP<uint32_t>(c->id[k]), charge != nullptr, acc != nullptr);
     NB_LAUNCHED(c, "upload");
     NB_CU(c, cudaStreamSynchronize(c->st));
+    c->n = n;
+    c->escapes = 0;
     c->time = 0.0;
     c->have_acc = acc != nullptr;
     c->amax_valid = false;
@@ -522,9 +542,9 @@ int nbody_diagnostics(nbody_ctx* c, double* out) {
 
 int nbody_get_stats(nbody_ctx* c, int64_t* out, int n) {
     if (!c || !out) return NBODY_ERR_INVALID;
-    const int64_t v[7] = {(int64_t)c->h_stats[0], (int64_t)c->h_stats[1], (int64_t)c->h_stats[2], c->nnodes,
-                          c->nleaves, c->depth, c->launches};
-    for (int i = 0; i < n && i < 7; ++i) out[i] = v[i];
+    const int64_t v[8] = {(int64_t)c->h_stats[0], (int64_t)c->h_stats[1], (int64_t)c->h_stats[2], c->nnodes,
+                          c->nleaves, c->depth, c->launches, c->escapes};
+    for (int i = 0; i < n && i < 8; ++i) out[i] = v[i];
     return NBODY_OK;
 }
 
@@ -645,6 +665,28 @@ int nbody_set_timestep_control(nbody_ctx* c, int mode, double eta, double length
     c->dt_max = dt_max;
     c->amax_valid = false;
     return NBODY_OK;
+}
+
+int nbody_set_escape_policy(nbody_ctx* c, int policy) {
+    if (!c) return NBODY_ERR_INVALID;
+    if (policy != NBODY_ESCAPE_GROW && policy != NBODY_ESCAPE_ERROR)
+        return nb_fail(c, NBODY_ERR_INVALID, "policy must be NBODY_ESCAPE_GROW or NBODY_ESCAPE_ERROR");
+    c->escape_policy = policy;
+    return NBODY_OK;
+}
+
+int nbody_set_wait_limits(nbody_ctx* c, int64_t scan_polls, int64_t copy_cycles) {
+    if (!c) return NBODY_ERR_INVALID;
+    c->scan_polls = scan_polls > 0 ? scan_polls : NB_SCAN_POLLS;
+    c->copy_cycles = copy_cycles > 0 ? (long long)copy_cycles : NB_COPY_CYCLES;
+    return NBODY_OK;
+}
+
+int nbody_selftest_wait(nbody_ctx* c, int which) {
+    if (!c) return NBODY_ERR_INVALID;
+    if (which != 0 && which != 1) return nb_fail(c, NBODY_ERR_INVALID, "which must be 0 (scan) or 1 (copy)");
+    NB_CU(c, cudaSetDevice(c->device));
+    return which == 0 ? nb_scan_wait_selftest(c) : nb_copy_wait_selftest(c);
 }
 
 int nbody_last_timestep(nbody_ctx* c, double* dt) {

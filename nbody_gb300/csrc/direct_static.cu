@@ -23,7 +23,12 @@
 //     each other's results: callers must order them.
 //   - the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, with that device current); make
-//     that first call before any stream capture on the device.
+//     that first call before any stream capture on the device.  A later call
+//     checks that the cached address still belongs to that device (after a
+//     cudaDeviceReset the module is loaded again and the address is looked up
+//     again);
+//   - the call selects `device` for its own launches and gives the calling
+//     thread back the device that was current before, on every return path.
 #include <mutex>
 
 #include "nbody_internal.cuh"
@@ -105,6 +110,48 @@ __global__ void k_direct_aos_final(int64_t n, int64_t nt, const int64_t* __restr
 // failures are reported like nbody_create's: nbody_last_error(NULL) returns the message
 int fail(int code, const char* msg) { return nb_fail(nullptr, code, msg); }
 
+
+// the device address of the scratch array on the current device (`device`), looked up once per
+// device and checked again on later calls: after a cudaDeviceReset the cached address is stale
+double* scratch_on(int device) {
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (g_static_ptr[device]) {
+        cudaPointerAttributes at;
+        const cudaError_t e = cudaPointerGetAttributes(&at, g_static_ptr[device]);
+        if (e == cudaSuccess && at.type == cudaMemoryTypeDevice && at.device == device) return g_static_ptr[device];
+        cudaGetLastError();
+        g_static_ptr[device] = nullptr;
+    }
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_direct_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    g_static_ptr[device] = (double*)p;
+    return g_static_ptr[device];
+}
+
+int direct_static(int device, int64_t n, const double* pos, const double* mass, const double* charge, double eps,
+                  double G, int64_t nt, const int64_t* targets, double* acc, double* pot, void* stream) {
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(NBODY_ERR_NO_DEVICE, "nbody_direct_forces_static: cannot select the device");
+    }
+    double* scratch = scratch_on(device);
+    if (!scratch) return fail(NBODY_ERR_CUDA, "nbody_direct_forces_static: cudaGetSymbolAddress failed");
+    int64_t ns = NB_STATIC_SLOTS / nt;
+    const int nsplit = (int)(ns > 64 ? 64 : (ns < 1 ? 1 : ns));
+    cudaStream_t st = (cudaStream_t)stream;
+    dim3 g((unsigned)((nt + ST - 1) / ST), (unsigned)nsplit);
+    k_direct_aos<<<g, ST, 0, st>>>(n, pos, charge ? charge : mass, nt, targets, nsplit, eps * eps, scratch);
+    k_direct_aos_final<<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(n, nt, targets, nsplit, scratch, mass,
+                                                                       charge ? charge : mass, G, acc, pot);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(NBODY_ERR_CUDA, cudaGetErrorString(e));
+    return NBODY_OK;
+}
+
 }  // namespace
 
 extern "C" int nbody_direct_forces_static(int device, int64_t n, const double* pos, const double* mass,
@@ -117,32 +164,15 @@ extern "C" int nbody_direct_forces_static(int device, int64_t n, const double* p
     if (device < 0 || device >= NB_STATIC_MAX_DEVICES)
         return fail(NBODY_ERR_INVALID, "nbody_direct_forces_static: device ordinal out of range");
     if (nt == 0) return NBODY_OK;
-    if (cudaSetDevice(device) != cudaSuccess) {
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) {
         cudaGetLastError();
-        return fail(NBODY_ERR_NO_DEVICE, "nbody_direct_forces_static: cannot select the device");
+        prev = -1;
     }
-    double* scratch;
-    {
-        std::lock_guard<std::mutex> lk(g_static_mu);
-        if (!g_static_ptr[device]) {
-            void* p = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&p, g_direct_scratch);
-            if (e != cudaSuccess || !p) {
-                cudaGetLastError();
-                return fail(NBODY_ERR_CUDA, "nbody_direct_forces_static: cudaGetSymbolAddress failed");
-            }
-            g_static_ptr[device] = (double*)p;
-        }
-        scratch = g_static_ptr[device];
+    const int rc = direct_static(device, n, pos, mass, charge, eps, G, nt, targets, acc, pot, stream);
+    if (prev >= 0 && prev != device) {
+        cudaSetDevice(prev);
+        cudaGetLastError();
     }
-    int64_t ns = NB_STATIC_SLOTS / nt;
-    const int nsplit = (int)(ns > 64 ? 64 : (ns < 1 ? 1 : ns));
-    cudaStream_t st = (cudaStream_t)stream;
-    dim3 g((unsigned)((nt + ST - 1) / ST), (unsigned)nsplit);
-    k_direct_aos<<<g, ST, 0, st>>>(n, pos, charge ? charge : mass, nt, targets, nsplit, eps * eps, scratch);
-    k_direct_aos_final<<<(unsigned)((nt + 127) / 128), 128, 0, st>>>(n, nt, targets, nsplit, scratch, mass,
-                                                                       charge ? charge : mass, G, acc, pot);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(NBODY_ERR_CUDA, cudaGetErrorString(e));
-    return NBODY_OK;
+    return rc;
 }

@@ -294,6 +294,7 @@ struct M2LArgs {
     int32_t* info;
     double eps2;
     int64_t nnodes;
+    long long wait_cycles;   // bound of each wait for this warp's bulk copies (SM clock cycles)
 };
 
 template <int MODE, int P>
@@ -334,15 +335,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// warp-uniform bounded wait (about a second at GB300 clocks); false on timeout
-__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity) {
+// warp-uniform bounded wait of at most `limit` SM clock cycles; false on timeout
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, long long limit) {
     const long long t0 = clock64();
     bool ok = false;
     for (;;) {
         ok = ok || mbar_try_wait(bar, parity);
         if (__all_sync(0xffffffffu, ok)) return true;
         const long long dt = __shfl_sync(0xffffffffu, clock64() - t0, 0);
-        if (dt > 2000000000ll) return false;
+        if (dt > limit) return false;
     }
 }
 
@@ -416,7 +417,7 @@ __global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A)
             sn_next = issue(b + 1, s_ahead);
             s_ahead = entry(b + 2);
         }
-        if (!mbar_wait_warp(&bar[k], (b >> 1) & 1)) { failed = true; b_fail = b; break; }
+        if (!mbar_wait_warp(&bar[k], (b >> 1) & 1, A.wait_cycles)) { failed = true; b_fail = b; break; }
         if ((uint32_t)lane < nb) {
             int sx, sy, sz;
             centre_fine32(sn, sx, sy, sz);
@@ -434,10 +435,12 @@ __global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A)
         __syncwarp();
     }
     if (failed) {
-        // let every copy already issued land before the shared memory is released
+        // let every copy already issued land before the shared memory is released (with the
+        // default bound, whatever the configured one: these copies are in flight)
         if (lane == 0) atomicOr((unsigned int*)&A.info[INFO_ERR], NB_ERRBIT_ASYNC);
-        mbar_wait_warp(&bar[b_fail & 1], (b_fail >> 1) & 1);
-        if (b_fail + 1 < nbatch) mbar_wait_warp(&bar[(b_fail + 1) & 1], ((b_fail + 1) >> 1) & 1);
+        mbar_wait_warp(&bar[b_fail & 1], (b_fail >> 1) & 1, NB_COPY_CYCLES);
+        if (b_fail + 1 < nbatch)
+            mbar_wait_warp(&bar[(b_fail + 1) & 1], ((b_fail + 1) >> 1) & 1, NB_COPY_CYCLES);
         return;
     }
     // lane-order butterfly sums; lane a % 32 keeps coefficient a and converts only its own
@@ -896,6 +899,7 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
         B.eps2 = c->prm.eps * c->prm.eps;
         B.nnodes = nn;
         B.info = DP<int32_t>(c->info);
+        B.wait_cycles = c->copy_cycles;
         constexpr int W = M2LSmem<MODE, P>::warps;
         const size_t smem = (size_t)W * M2LSmem<MODE, P>::per_warp;
         NB_CU(c, cudaFuncSetAttribute(k_m2l<MODE, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -16,11 +16,15 @@
 // error bits raised on the device (ctx->d_info[INFO_ERR])
 #define NB_ERRBIT_PEND_CAP 1u      // refinement list capacity exceeded
 #define NB_ERRBIT_P2P_CAP 2u       // near-field list capacity exceeded
-#define NB_ERRBIT_RANGE 8u         // a particle lay outside a fixed root box
+#define NB_ERRBIT_RANGE 8u         // no representable root box covers the particles
 #define NB_ERRBIT_NONFINITE 16u    // a position was not finite
 #define NB_ERRBIT_M2L_CAP 32u      // far-field list capacity exceeded
 #define NB_ERRBIT_ASYNC 64u        // an asynchronous copy did not complete within its time limit
 #define NB_ERRBIT_ITEM_CAP 128u    // list-building work items exceeded their capacity
+#define NB_ERRBIT_ESCAPE 256u      // a particle lay outside the fixed root box
+
+#define NB_SCAN_POLLS (1ll << 20)  // default look-back polls of one scan status word (about a second)
+#define NB_COPY_CYCLES 2000000000ll   // default bound of the far-field kernel's copy waits (SM cycles)
 
 #define NB_P2P_CHUNK 256           // partner leaves per near-field work item
 #define NB_P2P_CLASSES 6           // near-field leaf-size classes (one kernel each)
@@ -120,6 +124,9 @@ struct nbody_ctx {
     DevBuf keys[2], vals[2], hist, hist_scan;
     DevBuf scan_part;              // single-pass scan state: ticket counter and tile status words
     uint64_t scan_epoch = 0;       // tag of the last scan's status words
+    int64_t scan_polls = NB_SCAN_POLLS;            // look-back polls of one status word before giving up
+    long long copy_cycles = NB_COPY_CYCLES;        // far-field wait for its bulk copies (SM clock cycles)
+    DevBuf wait_probe;             // status words of nbody_selftest_scan_wait
 
     // tree scratch and result
     DevBuf cpl, wnd, leaflvl, nc, pfx, seedk[2], seedv[2], nodes, leafflag, leafpfx, leaves;
@@ -141,6 +148,8 @@ struct nbody_ctx {
     unsigned long long h_stats[8] = {0};
     int64_t launches = 0;          // kernels launched by the last force evaluation
     size_t dev_bytes = 0, dev_peak = 0;   // device memory held by the context, and its high-water mark
+    long long alloc_fail_after = -1;      // NBODY_FAIL_ALLOC_AFTER: allocations that succeed before one fails
+    long long alloc_calls = 0;
 
     // small device blocks + pinned mirrors
     DevBuf info, box, bbox;
@@ -165,6 +174,10 @@ struct nbody_ctx {
     float phase_ms[16] = {0};
 
     nb_traj* traj = nullptr;       // open trajectory file, if any
+
+    // particles leaving a fixed root box (nbody_set_escape_policy)
+    int escape_policy = NBODY_ESCAPE_GROW;
+    int64_t escapes = 0;           // evaluations since nbody_set_state that took a grown root box
 
     // step-size control (nbody_set_timestep_control)
     int dt_mode = NBODY_DT_FIXED;
@@ -203,6 +216,13 @@ int nb_scan_u32(nbody_ctx* c, const uint32_t* in, uint32_t* out, int64_t n, uint
 // first *n_dev of the n entries are scanned
 int nb_scan3_u32(nbody_ctx* c, const uint32_t* const in[3], uint32_t* const out[3], int64_t n,
                  uint32_t* const total_dev[3], const uint32_t* n_dev = nullptr);
+// the scan look-back's wait on a word nothing publishes; NBODY_ERR_CUDA once it ran out (sort.cu)
+int nb_scan_wait_selftest(nbody_ctx* c);
+// the far-field kernel's copy wait on a barrier no copy completes; NBODY_ERR_CUDA once it ran out
+// (fmm_fp32.cu)
+int nb_copy_wait_selftest(nbody_ctx* c);
+// NBODY_ERR_CUDA if h_info[INFO_ERR] (just read back) says a far-field copy wait ran out (api.cu)
+int nb_check_async(nbody_ctx* c);
 int nb_radix_sort(nbody_ctx* c, int64_t n, uint64_t* k0, uint32_t* v0, uint64_t* k1, uint32_t* v1, int begin_bit,
                   int end_bit, int* result_in_first);
 

@@ -45,7 +45,6 @@ __device__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
 // sums are integer, so the result does not depend on which words a block happened to see.
 constexpr uint32_t SCAN_EPOCH_SHIFT = 34;
 constexpr uint64_t SCAN_FLAG_SUM = 1ull << 32, SCAN_FLAG_INCL = 2ull << 32;
-constexpr int SCAN_SPIN_LIMIT = 1 << 20;        // polls of one status word before giving up (~1 s)
 
 struct ScanK {
     const uint32_t* in[3];         // null: array unused
@@ -56,6 +55,7 @@ struct ScanK {
     int64_t nb;                    // blocks of this launch (tiles of n entries)
     uint64_t epoch;
     int32_t* info;                 // INFO_SCAN_ERR is raised when a look-back gives up
+    int64_t spin_limit;            // polls of one status word before giving up
 };
 
 __device__ __forceinline__ int64_t scan_len(const ScanK& A, int64_t n) {
@@ -74,7 +74,8 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
 }
 
 // one warp: publishes tile t's sum `agg`, returns the sum of all tiles before t (every lane)
-__device__ uint32_t scan_lookback(unsigned long long* st, int64_t t, uint32_t agg, uint64_t epoch, int32_t* info) {
+__device__ uint32_t scan_lookback(unsigned long long* st, int64_t t, uint32_t agg, uint64_t epoch, int32_t* info,
+                                  int64_t spin_limit) {
     const int lane = lane_id();
     const unsigned long long tag = epoch << SCAN_EPOCH_SHIFT;
     if (t == 0) {
@@ -91,8 +92,8 @@ __device__ uint32_t scan_lookback(unsigned long long* st, int64_t t, uint32_t ag
         uint32_t val = 0;
         if (my >= 0) {
             unsigned long long w = ld_relaxed_u64(st + my);
-            int spins = 0;
-            while ((w >> SCAN_EPOCH_SHIFT) != epoch && ++spins < SCAN_SPIN_LIMIT) {
+            int64_t spins = 0;
+            while ((w >> SCAN_EPOCH_SHIFT) != epoch && ++spins < spin_limit) {
                 __nanosleep(64);
                 w = ld_relaxed_u64(st + my);
             }
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(ScanK A, int64_t n) {
 #pragma unroll
     for (int a = 0; a < K; ++a)
         if (warp == a && A.in[a]) {
-            const uint32_t pre = scan_lookback(A.state + 1 + a * A.nb, t, agg[a], A.epoch, A.info);
+            const uint32_t pre = scan_lookback(A.state + 1 + a * A.nb, t, agg[a], A.epoch, A.info, A.spin_limit);
             if (lane_id() == 0) s_prefix[a] = pre;
         }
     __syncthreads();
@@ -226,6 +227,12 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_scatter(const uint64_t*
     }
 }
 
+// the look-back's wait on a status word that nothing publishes (word 0 of `st` holds epoch 0, which
+// no scan uses): tile 1 polls it until the limit runs out and raises INFO_SCAN_ERR
+__global__ void k_scan_wait_selftest(unsigned long long* st, int32_t* info, int64_t spin_limit) {
+    scan_lookback(st, 1, 1u, 1u, info, spin_limit);
+}
+
 }  // namespace
 
 namespace {
@@ -252,6 +259,7 @@ int scan_launch(nbody_ctx* c, const uint32_t* const* in, uint32_t* const* out, i
     c->scan_epoch = c->scan_epoch % ((1ull << 30) - 1) + 1;     // 1 .. 2^30 - 1; 0 marks a cleared word
     A.epoch = c->scan_epoch;
     A.info = DP<int32_t>(c->info);
+    A.spin_limit = c->scan_polls;
     k_scan<K><<<(unsigned)nb, SCAN_THREADS, 0, c->st>>>(A, n);
     NB_LAUNCHED(c, "scan");
     c->launches += 1;
@@ -303,5 +311,17 @@ int nb_radix_sort(nbody_ctx* c, int64_t n, uint64_t* k0, uint32_t* v0, uint64_t*
         uint32_t* tv = vi; vi = vo; vo = tv;
         *result_in_first = !*result_in_first;
     }
+    return NBODY_OK;
+}
+
+int nb_scan_wait_selftest(nbody_ctx* c) {
+    NB_TRY(nb_grow(c, c->wait_probe, 2 * sizeof(unsigned long long)));
+    NB_CU(c, cudaMemsetAsync(c->wait_probe.p, 0, 2 * sizeof(unsigned long long), c->st));
+    k_scan_wait_selftest<<<1, 32, 0, c->st>>>(DP<unsigned long long>(c->wait_probe), DP<int32_t>(c->info),
+                                              c->scan_polls);
+    NB_LAUNCHED(c, "scan wait self-test");
+    NB_CU(c, cudaMemcpyAsync(c->h_info, c->info.p, sizeof(int32_t) * INFO_WORDS, cudaMemcpyDeviceToHost, c->st));
+    NB_CU(c, cudaStreamSynchronize(c->st));
+    if (c->h_info[INFO_SCAN_ERR]) return nb_fail(c, NBODY_ERR_CUDA, "a device scan did not complete in time");
     return NBODY_OK;
 }

@@ -94,6 +94,16 @@ int nb_traj_capture(nbody_ctx* c) {
         T->busy[k] = true;
     }
     T->next = (k + 1) % nb_traj::SLOTS;
+    // slot k is ours until it is queued: on a failure below, hand it back before returning so a
+    // later capture does not wait for a row that will never be written
+    auto release_slot = [&](int rc) {
+        {
+            std::lock_guard<std::mutex> lk(T->mu);
+            T->busy[k] = false;
+        }
+        T->cv.notify_all();
+        return rc;
+    };
     double* st = DP<double>(c->stage);
     const int cur = c->cur;
     const unsigned g = (unsigned)((c->n + TB - 1) / TB);
@@ -103,9 +113,11 @@ int nb_traj_capture(nbody_ctx* c) {
     else
         k_traj_positions<double><<<g, TB, 0, c->st>>>(c->n, T->order, DP<double>(c->x[cur]), DP<double>(c->y[cur]),
                                                       DP<double>(c->z[cur]), DP<uint32_t>(c->id[cur]), st);
-    NB_LAUNCHED(c, "trajectory positions");
-    NB_CU(c, cudaMemcpyAsync(T->slot[k], st, sizeof(double) * 3 * c->n, cudaMemcpyDeviceToHost, c->st));
-    NB_CU(c, cudaEventRecord(T->ready[k], c->st));
+    if (int rc = nb_cuda(c, cudaGetLastError(), "trajectory positions")) return release_slot(rc);
+    if (int rc = nb_cuda(c, cudaMemcpyAsync(T->slot[k], st, sizeof(double) * 3 * c->n, cudaMemcpyDeviceToHost, c->st),
+                         "trajectory copy"))
+        return release_slot(rc);
+    if (int rc = nb_cuda(c, cudaEventRecord(T->ready[k], c->st), "trajectory event")) return release_slot(rc);
     T->slot_time[k] = c->time;
     {
         std::lock_guard<std::mutex> lk(T->mu);

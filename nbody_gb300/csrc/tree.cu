@@ -103,9 +103,39 @@ __global__ void __launch_bounds__(TB) k_kick_drift_bbox(int64_t n, StatePtrs<R> 
     if (bad) atomicOr((unsigned int*)&info[INFO_ERR], NB_ERRBIT_NONFINITE);
 }
 
-// root box: fixed (the reference's [0, bounds)) or the power-of-two data cube
-__global__ void k_box(const unsigned long long* bbox, int fixed, double fx, double fy, double fz, double fside,
-                      BoxDev* box, int32_t* info) {
+// Root box of a fixed-box run that a particle has left (escape policy NBODY_ESCAPE_GROW): the
+// smallest box of side fside * 2^j whose cells of level j include the fixed box itself, with origin
+// f - a * fside per axis (a >= 0 integer), that covers [lo, hi].  Inside the fixed box the cells
+// below level j are the fixed box's own cells, so particles there are binned as before (the keys
+// lose their j lowest levels).  false if no such box is representable.
+__device__ bool grown_box(const double* lo, const double* hi, const double* f, double fside, double* o,
+                          double* side) {
+    double a[3];
+    for (int d = 0; d < 3; ++d) {
+        a[d] = lo[d] < f[d] ? ceil((f[d] - lo[d]) / fside) : 0.0;
+        // rounding of the quotient: step until the origin is at or below the lowest coordinate
+        for (int it = 0; it < 4 && f[d] - a[d] * fside > lo[d]; ++it) a[d] += 1.0;
+        o[d] = f[d] - a[d] * fside;
+        if (!(o[d] <= lo[d])) return false;
+    }
+    double s = fside;
+    for (int j = 0; j <= 1100 && isfinite(s); ++j) {
+        bool ok = true;
+        for (int d = 0; d < 3; ++d) ok = ok && (a[d] * fside < s) && (o[d] + s > hi[d]);
+        if (ok) {
+            *side = s;
+            return true;
+        }
+        s *= 2.0;
+    }
+    return false;
+}
+
+// root box: fixed (the reference's [0, bounds)) or the power-of-two data cube.  A particle outside
+// a fixed box raises NB_ERRBIT_ESCAPE; with grow = 1 the step takes grown_box instead, with
+// grow = 0 the box stays (the host then fails the step with NBODY_ERR_RANGE).
+__global__ void k_box(const unsigned long long* bbox, int fixed, int grow, double fx, double fy, double fz,
+                      double fside, BoxDev* box, int32_t* info) {
     double lo[3], hi[3];
     for (int d = 0; d < 3; ++d) {
         lo[d] = ord_val(bbox[d]);
@@ -122,8 +152,16 @@ __global__ void k_box(const unsigned long long* bbox, int fixed, double fx, doub
     } else if (fixed) {
         b.ox = fx; b.oy = fy; b.oz = fz; b.side = fside;
         if (lo[0] < fx || lo[1] < fy || lo[2] < fz || hi[0] >= fx + fside || hi[1] >= fy + fside ||
-            hi[2] >= fz + fside)
-            atomicOr((unsigned int*)&info[INFO_ERR], NB_ERRBIT_RANGE);
+            hi[2] >= fz + fside) {
+            atomicOr((unsigned int*)&info[INFO_ERR], NB_ERRBIT_ESCAPE);
+            const double f[3] = {fx, fy, fz};
+            double o[3], side;
+            if (grow && grown_box(lo, hi, f, fside, o, &side)) {
+                b.ox = o[0]; b.oy = o[1]; b.oz = o[2]; b.side = side;
+            } else if (grow) {
+                atomicOr((unsigned int*)&info[INFO_ERR], NB_ERRBIT_RANGE);
+            }
+        }
     } else {
         double ext = fmax(fmax(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]) * (1.0 + 0x1p-20);
         double side = 1.0;
@@ -333,8 +371,9 @@ int begin_step_t(nbody_ctx* c, int kdk) {
     if (g == 0) g = 1;
     k_kick_drift_bbox<R><<<g, TB, 0, c->st>>>(n, state<R>(c, c->cur), 0.5 * c->prm.dt, c->prm.dt, kdk, bb,
                                               DP<int32_t>(c->info));
-    k_box<<<1, 1, 0, c->st>>>(bb, c->prm.fixed_box, c->prm.box_min[0], c->prm.box_min[1], c->prm.box_min[2],
-                              c->prm.box_size, DP<BoxDev>(c->box), DP<int32_t>(c->info));
+    k_box<<<1, 1, 0, c->st>>>(bb, c->prm.fixed_box, c->escape_policy == NBODY_ESCAPE_GROW, c->prm.box_min[0],
+                              c->prm.box_min[1], c->prm.box_min[2], c->prm.box_size, DP<BoxDev>(c->box),
+                              DP<int32_t>(c->info));
     k_keys<R><<<nblk(n), TB, 0, c->st>>>(n, DP<R>(c->x[c->cur]), DP<R>(c->y[c->cur]), DP<R>(c->z[c->cur]),
                                          DP<BoxDev>(c->box), DP<uint64_t>(c->keys[0]), DP<uint32_t>(c->vals[0]));
     NB_LAUNCHED(c, "kick_drift_keys");
@@ -383,8 +422,14 @@ int nb_build_tree(nbody_ctx* c) {
     NB_CU(c, cudaMemcpyAsync(c->h_info, info, sizeof(int32_t) * INFO_WORDS, cudaMemcpyDeviceToHost, c->st));
     NB_CU(c, cudaStreamSynchronize(c->st));
     if (c->h_info[INFO_SCAN_ERR]) return nb_fail(c, NBODY_ERR_CUDA, "a device scan did not complete in time");
-    if ((uint32_t)c->h_info[INFO_ERR] & NB_ERRBIT_NONFINITE)
-        return nb_fail(c, NBODY_ERR_STATE, "non-finite particle position");
+    const uint32_t err = (uint32_t)c->h_info[INFO_ERR];
+    if (err & NB_ERRBIT_NONFINITE) return nb_fail(c, NBODY_ERR_STATE, "non-finite particle position");
+    if (err & NB_ERRBIT_ESCAPE) {
+        if (c->escape_policy == NBODY_ESCAPE_ERROR)
+            return nb_fail(c, NBODY_ERR_RANGE, "a particle left the fixed root box");
+        ++c->escapes;
+    }
+    if (err & NB_ERRBIT_RANGE) return nb_fail(c, NBODY_ERR_RANGE, "no representable root box covers the particles");
     c->nnodes = (uint32_t)c->h_info[INFO_NNODES];
     c->nleaves = c->h_info[INFO_NLEAVES];
     c->depth = c->h_info[INFO_DEPTH];

@@ -257,10 +257,22 @@ class CudaSimulation:
         return cur.value, peak.value
 
     def stats(self):
-        out = np.zeros(7, np.int64)
-        check(self._h, _lib.load().nbody_get_stats(self._h, ptr(out), 7))
-        keys = ("m2l_pairs", "p2p_particle_pairs", "p2p_leaf_pairs", "nodes", "leaves", "depth", "launches")
+        out = np.zeros(8, np.int64)
+        check(self._h, _lib.load().nbody_get_stats(self._h, ptr(out), 8))
+        keys = ("m2l_pairs", "p2p_particle_pairs", "p2p_leaf_pairs", "nodes", "leaves", "depth", "launches",
+                "grown_boxes")
         return dict(zip(keys, (int(v) for v in out)))
+
+    def set_escape_policy(self, policy: str = "grow"):
+        """What an evaluation does when a particle lies outside a fixed root box: "grow" takes the
+        smallest power-of-two multiple of the box that has it as a cell and covers every particle;
+        "error" fails with NbodyError (code 7)."""
+        p = {"grow": _lib.ESCAPE_GROW, "error": _lib.ESCAPE_ERROR}[policy]
+        check(self._h, _lib.load().nbody_set_escape_policy(self._h, p))
+
+    def set_wait_limits(self, scan_polls: int = 0, copy_cycles: int = 0):
+        """Bounds of the device-side waits (<= 0: the defaults of about a second)."""
+        check(self._h, _lib.load().nbody_set_wait_limits(self._h, int(scan_polls), int(copy_cycles)))
 
     def set_timing(self, on: bool = True):
         check(self._h, _lib.load().nbody_set_timing(self._h, int(on)))

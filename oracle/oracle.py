@@ -28,13 +28,23 @@ _u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 _u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
 
 
+def reference_dir() -> str:
+    """Where the reference tree is mounted: $NBODY_REFERENCE_DIR, else the Makefile's default."""
+    env = os.environ.get("NBODY_REFERENCE_DIR")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
 def build(ref: bool | None = None) -> None:
     """Compile liboracle.so (and, if the reference is mounted, libnbody_ref.so)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    rdir = reference_dir()
     if ref is None:
-        ref = os.path.isdir("/root/reference/src")
+        ref = bool(rdir) and os.path.isdir(os.path.join(rdir, "src"))
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={rdir}"], check=True)
 
 
 def lib():
@@ -208,6 +218,60 @@ def bounding_box(pos):
         if np.all(origin + side > hi):
             return np.array([origin[0], origin[1], origin[2], side])
         side *= 2.0
+
+
+def grown_box(pos, fixed):
+    """Root box of a step whose particles leave the fixed box (fx, fy, fz, side), policy "grow".
+
+    Restates the library's rule for particles outside the reference's [0, bounds) root box (the
+    reference leaves that case to its external octree, src/open_cl_simulation.cpp:43-47,120-123):
+    per axis the origin moves down by a whole number a of box sides until it is at or below the
+    lowest coordinate, then the side doubles until every coordinate is below origin + side, so the
+    fixed box stays one cell of the grown box.  Returns the fixed box itself if nothing left it.
+    """
+    pos = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
+    f = np.asarray(fixed[:3], dtype=np.float64)
+    fs = float(fixed[3])
+    lo, hi = pos.min(axis=0), pos.max(axis=0)
+    if np.all(lo >= f) and np.all(hi < f + fs):
+        return np.array([f[0], f[1], f[2], fs])
+    o = np.zeros(3)
+    a = np.zeros(3)
+    for d in range(3):
+        a[d] = np.ceil((f[d] - lo[d]) / fs) if lo[d] < f[d] else 0.0
+        it = 0
+        while it < 4 and f[d] - a[d] * fs > lo[d]:
+            a[d] += 1.0
+            it += 1
+        o[d] = f[d] - a[d] * fs
+    s = fs
+    while not all(a[d] * fs < s and o[d] + s > hi[d] for d in range(3)):
+        s *= 2.0
+    return np.array([o[0], o[1], o[2], s])
+
+
+def ref_mode_run(pos, vel, q, m, box, cap, theta, eps, dt, steps, escape="grow"):
+    """The reference's FMM step repeated: order 0 (monopole about the geometric centre, constant
+    local field), FP32 arithmetic, explicit Euler v += F/m dt, x += v_old dt
+    (src/open_cl_simulation.cpp:572-616, src/field.cl, src/force.cl), the octree rebuilt every
+    step over the fixed root box (grown by grown_box when a particle has left it).  Inputs and
+    outputs are in input order; returns (pos, vel) as float32."""
+    x = np.asarray(pos, dtype=np.float32).reshape(-1, 3).copy()
+    v = np.asarray(vel, dtype=np.float32).reshape(-1, 3).copy()
+    q64 = np.asarray(q, dtype=np.float64)
+    m64 = np.asarray(m, dtype=np.float64)
+    m32 = m64.astype(np.float32)[:, None]
+    dt32 = np.float32(dt)
+    for _ in range(steps):
+        b = grown_box(x.astype(np.float64), box) if escape == "grow" else np.asarray(box, np.float64)
+        t = Tree(x.astype(np.float64), q64, m64, box=b, cap=cap).traverse(theta)
+        fl, fn = t.ref_forces_f32(eps)
+        F = (fl + fn).astype(np.float32)
+        v_old = v.copy()
+        v = v + (F / m32) * dt32
+        x = x + v_old * dt32
+        del t
+    return x, v
 
 
 def direct(pos, q=None, m=None, eps=0.01, G=1.0, targets=None, nthreads=None):

@@ -30,7 +30,8 @@ def test_cpp_drop_in_matches_python_binding(nb, tmp_path):
     data[:, 7] = rng.uniform(0.1, 1, n)
     f = tmp_path / "particles.f32"
     data.tofile(f)
-    out = subprocess.run([str(exe), str(n), str(steps), str(f)], check=True, capture_output=True, text=True).stdout
+    out = subprocess.run([str(exe), str(n), str(steps), str(f), "1e-5"], check=True, capture_output=True,
+                         text=True).stdout
     fields = out.split()
     t_cpp, count, checksum = float(fields[1]), int(fields[3]), float(fields[5])
     # the same run through the Python binding (reference defaults, box [0, 1), dt 1e-5)
@@ -42,6 +43,49 @@ def test_cpp_drop_in_matches_python_binding(nb, tmp_path):
     assert count == n
     assert abs(t_cpp - np.float32(t)) == 0
     assert abs(checksum - ref) <= 1e-12 * abs(ref)
+
+
+def _build_drop_in(tmp_path):
+    cxx = shutil.which("g++")
+    assert cxx, "g++ is needed to build the C++ drop-in test"
+    from nbody_gb300 import _lib
+    exe = tmp_path / "drop_in"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    subprocess.run([cxx, "-std=c++14", "-O2", "-Wall", "-Wextra", "-pedantic", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "drop_in_main.cpp"), "-L", libdir, "-lnbody_gb300",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    return exe
+
+
+def test_cpp_drop_in_reference_parameters(nb, oracle, tmp_path):
+    """The reference's own main.cpp workload (N uniform in [0, 1), |v| <= 0.1, masses 1..10, charges
+    0.1..1, dt 1e-3, reference defaults: order 1, FP32, explicit Euler, capacity 8) for 10 steps at
+    N = 100,000.  The charges repel and particles leave [0, 1) within these steps; the escape policy
+    grows the root box.  On the final state the library's tree, interaction sets and forces match the
+    oracle's restated reference FMM on the same grown box (forces within 1e-5 of the largest)."""
+    exe = _build_drop_in(tmp_path)
+    n, steps = 100000, 10
+    fin = tmp_path / "final.f32"
+    out = subprocess.run([str(exe), str(n), str(steps), "-", "1e-3", str(fin)], check=True, capture_output=True,
+                         text=True).stdout.split()
+    assert int(out[3]) == n and abs(float(out[1]) - 1e-2) < 1e-6
+    assert int(out[7]) > 0, "no particle left the box: the escape path was not exercised"
+    d = np.fromfile(fin, np.float32).reshape(n, 8).astype(np.float64)
+    pos, vel, m, q = d[:, :3], d[:, 3:6], d[:, 6], d[:, 7]
+    assert np.all(np.isfinite(pos))
+    assert (pos < 0).any() or (pos >= 1).any()
+    sim = nb.CudaSimulation([1.0, 1.0, 1.0, 0.0], None, 1e-3)
+    sim.set_state(pos, vel, m, q)
+    acc = sim.forces()
+    assert sim.stats()["grown_boxes"] == 1
+    box = oracle.grown_box(pos, [0.0, 0.0, 0.0, 1.0])
+    keys, perm, nodes = sim.tree()
+    t = oracle.Tree(pos, q, m, box=box, cap=8).traverse(0.5)
+    np.testing.assert_array_equal(perm, t.perm.astype(np.int64))
+    np.testing.assert_array_equal(nodes, t.nodes)
+    fl, fn = t.ref_forces_f32(0.01)
+    F, Fref = acc * m[:, None], (fl + fn).astype(np.float64)
+    assert np.abs(F - Fref).max() <= 1e-5 * np.abs(Fref).max()
 
 
 def test_cpp_adjoint_matches_python_binding(nb, tmp_path):

@@ -265,3 +265,73 @@ def test_list_capacity_retry_small_theta(nb, oracle):
     a_ref, _ = t.fmm(3, 0.01)
     assert _rel_rms(acc, a_ref) < 3e-6
     assert sim.stats()["p2p_leaf_pairs"] == len(t.pairs("p2p"))
+
+
+def test_direct_sum_matches_oracle(nb, oracle):
+    """The device FP64 direct sum (the accuracy reference of every force-error figure) against the
+    oracle's FP64 direct sum: 1e-12 relative per target (acceleration) and of the largest potential."""
+    rng = np.random.default_rng(44)
+    pos, vel, m = ics.plummer(20000, seed=44)
+    q = m * rng.uniform(0.5, 1.5, len(m))
+    tg = rng.choice(len(m), 2048, replace=False)
+    sim = nb.CudaSimulation.from_arrays(pos, vel, m, q, precision=nb.PREC_FP64, fixed_box=0, eps=0.01, G=0.7)
+    acc, pot = sim.direct(tg)
+    a_ref, p_ref = oracle.direct(pos, q, m, eps=0.01, G=0.7, targets=tg)
+    err = np.linalg.norm(acc - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+    assert err.max() < 1e-12, err.max()
+    assert np.abs(pot - p_ref).max() < 1e-12 * np.abs(p_ref).max()
+
+
+def _escaped(n, seed):
+    """Particles of a unit cube, a few of them pushed out through different faces."""
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(0, 1, (n, 3))
+    pos[:5] = [[-0.3, 0.5, 0.5], [0.5, 1.7, 0.5], [0.5, 0.5, -2.2], [1.0, 0.2, 0.2], [0.1, 0.9, 0.999999]]
+    m = rng.uniform(1, 10, n)
+    q = rng.uniform(0.1, 1, n)
+    # values the FP32 state holds exactly, so the oracle bins the same coordinates
+    f32 = lambda a: a.astype(np.float32).astype(np.float64)
+    return f32(pos), f32(m), f32(q)
+
+
+def test_escape_policy_grow_matches_oracle(nb, oracle):
+    """Reference mode on [0, 1): particles outside the box take the grown root box of oracle.grown_box;
+    tree and interaction sets bit-exact, forces within 1e-5 of the largest (the reference-kernel
+    tolerance), and the evaluation is counted."""
+    pos, m, q = _escaped(6000, 45)
+    sim = nb.CudaSimulation([1.0, 1.0, 1.0, 0.0], None, 1e-3)
+    sim.set_state(pos, None, m, q)
+    acc = sim.forces()
+    assert sim.stats()["grown_boxes"] == 1
+    box = oracle.grown_box(pos, [0.0, 0.0, 0.0, 1.0])
+    assert box[3] == 4.0 and tuple(box[:3]) == (-1.0, 0.0, -3.0), box
+    keys, perm, nodes = sim.tree()
+    t = oracle.Tree(pos, q, m, box=box, cap=8).traverse(0.5)
+    np.testing.assert_array_equal(perm, t.perm.astype(np.int64))
+    np.testing.assert_array_equal(nodes, t.nodes)
+    assert _set(sim.interactions("p2p")) == _set(t.pairs("p2p"))
+    assert _set(sim.interactions("m2l")) == _set(t.pairs("m2l"))
+    fl, fn = t.ref_forces_f32(0.01)
+    F, Fref = acc * m[:, None], (fl + fn).astype(np.float64)
+    assert np.abs(F - Fref).max() <= 1e-5 * np.abs(Fref).max()
+    # inside the box again: the fixed box, nothing counted
+    sim.set_state(np.clip(pos, 0.0, 0.99), None, m, q)
+    sim.forces()
+    assert sim.stats()["grown_boxes"] == 0
+
+
+def test_escape_policy_error(nb):
+    pos, m, q = _escaped(3000, 46)
+    sim = nb.CudaSimulation([1.0, 1.0, 1.0, 0.0], None, 1e-3)
+    sim.set_escape_policy("error")
+    sim.set_state(pos, None, m, q)
+    with pytest.raises(nb.NbodyError) as e:
+        sim.forces()
+    assert e.value.code == 7
+    # explicit Euler: a failed step leaves the state as it was
+    before = sim.state("input")[0]
+    with pytest.raises(nb.NbodyError):
+        sim.step()
+    np.testing.assert_array_equal(sim.state("input")[0], before)
+    sim.set_escape_policy("grow")
+    assert np.all(np.isfinite(sim.forces()))

@@ -317,3 +317,28 @@ def test_adaptive_dt_rule(oracle):
     assert oracle.adaptive_dt(acc, 0.1, 0.05, 1e-6, 1e-3) == 1e-3       # clamped above
     assert oracle.adaptive_dt(acc, 1e-9, 0.05, 1e-6, 1.0) == 1e-6       # clamped below
     assert oracle.adaptive_dt(np.zeros((4, 3)), 0.1, 0.05, 1e-6, 0.5) == 0.5   # no acceleration: dt_max
+
+
+def test_grown_box_rule(oracle):
+    """oracle.grown_box: the fixed box is one cell of the grown box, which covers every point and is
+    the smallest such box (half its side would not cover them)."""
+    import numpy as np
+    fixed = [0.0, 0.0, 0.0, 1.0]
+    rng = np.random.default_rng(5)
+    inside = rng.uniform(0, 1, (100, 3))
+    assert list(oracle.grown_box(inside, fixed)) == fixed
+    pts = np.array([[-0.3, 0.5, 0.5], [0.5, 1.7, 0.5], [0.5, 0.5, -2.2], [1.0, 0.2, 0.2]])
+    assert list(oracle.grown_box(pts, fixed)) == [-1.0, 0.0, -3.0, 4.0]
+    for trial in range(200):
+        # dyadic corners, so the origin arithmetic is exact and the cell test below can be exact too
+        f = np.array([*(rng.integers(-128, 128, 3) / 64.0), 2.0 ** rng.integers(-3, 4)])
+        p = f[:3] + f[3] * rng.normal(0.5, rng.uniform(0.1, 8), (50, 3))
+        o0, o1, o2, s = oracle.grown_box(p, f)
+        o = np.array([o0, o1, o2])
+        assert np.all(o <= p.min(axis=0)) and np.all(o + s > p.max(axis=0))
+        k = s / f[3]
+        assert k >= 1 and k == 2.0 ** round(np.log2(k))
+        a = (f[:3] - o) / f[3]
+        assert np.all(a == np.round(a)) and np.all(a >= 0) and np.all(a < k)
+        if k > 1:
+            assert not (np.all(a < k / 2) and np.all(o + s / 2 > p.max(axis=0)))
