@@ -178,6 +178,22 @@ int nbody_forward_checkpointed(nbody_ctx* c, int nsteps, int every, double* t_ou
 int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* gx0, double* gv0, double* gq,
                    double* gm);
 
+/* Frozen-structure replay of the run recorded by nbody_forward_checkpointed
+   with every = 0: from the initial state given here (input order; vel and
+   charge may be NULL = zero velocity, charge = mass) it advances nsteps
+   (<= the recorded steps; < 0: all of them) leapfrog steps in which the
+   force evaluation at time point k reuses the tree, interaction lists and
+   near-field plan recorded at time point k, recomputing everything that
+   depends on the particle data.  That is the function whose derivative
+   nbody_backward returns, so central finite differences of the replay check
+   the adjoint without the jumps a rebuilt tree makes when a perturbed
+   particle crosses a cell boundary.  pos_out / vel_out (n x 3, input order,
+   may be NULL) receive the final state.  The recording and the context's
+   state are those of the recorded run again on return.  (No counterpart in
+   the reference.) */
+int nbody_forward_replay(nbody_ctx* c, const double* pos, const double* vel, const double* mass,
+                         const double* charge, int nsteps, double* pos_out, double* vel_out);
+
 /* Trajectory file (replaces the CSV dump of src/main.cpp:77-101, same row
    format: the time, then x,y,z of every particle, comma separated, one row per
    written step).  After nbody_trajectory_open, every `every`-th step taken by

@@ -43,6 +43,28 @@ __global__ void k_rev_drift(int64_t n, R* __restrict__ lv, const R* __restrict__
     if (i < n) lv[i] += (R)dt * lx[i];
 }
 
+// row_of[id[i]] = i: where each particle sits in the order of `id`
+__global__ void k_row_of(int64_t n, const uint32_t* __restrict__ id, uint32_t* __restrict__ row_of) {
+    const int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x;
+    if (i < n) row_of[id[i]] = (uint32_t)i;
+}
+
+// positions, velocities, masses and charges of buffer `a` (rows located by row_of) re-ordered into
+// the order id_new of buffer `b`
+template <typename R>
+struct Arr8 {
+    R* p[8];
+};
+template <typename R>
+__global__ void k_reorder(int64_t n, const uint32_t* __restrict__ id_new, const uint32_t* __restrict__ row_of,
+                          Arr8<R> a, Arr8<R> b) {
+    const int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t j = row_of[id_new[i]];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) b.p[k][i] = a.p[k][j];
+}
+
 // snapshot layout: 11 state arrays of n scalars (x y z vx vy vz ax ay az m q) then n ids
 size_t snapshot_bytes(const nbody_ctx* c) {
     const size_t b = (11 * c->rsz + sizeof(uint32_t)) * (size_t)c->n;
@@ -183,6 +205,7 @@ int rec_save(nbody_ctx* c, int j) {
     R.nn = c->nnodes;
     R.nl = c->nleaves;
     R.depth = c->depth;
+    R.box_side = c->box_side;
     std::copy(c->level_start, c->level_start + NB_LEVELS + 3, R.level_start);
     std::copy(c->h_info, c->h_info + INFO_WORDS, R.info);
     return NBODY_OK;
@@ -204,6 +227,7 @@ int rec_load(nbody_ctx* c, int j) {
     c->nnodes = R.nn;
     c->nleaves = R.nl;
     c->depth = R.depth;
+    c->box_side = R.box_side;
     std::copy(R.level_start, R.level_start + NB_LEVELS + 3, c->level_start);
     std::copy(R.info, R.info + INFO_WORDS, c->h_info);
     const int64_t npart = (uint32_t)R.info[INFO_P2P_PART];
@@ -283,6 +307,80 @@ int nbody_forward_checkpointed(nbody_ctx* c, int nsteps, int every, double* t_ou
     c->tree_at_final = true;
     if (t_out) *t_out = c->time;
     return NBODY_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// buffer `from` (ordered by its ids) -> buffer c->cur in the order of c->id[c->cur]
+template <typename R>
+int reorder_t(nbody_ctx* c, int from) {
+    const int k = c->cur;
+    const int64_t n = c->n;
+    uint32_t* row_of = DP<uint32_t>(c->pfx);          // tree scratch, free between evaluations
+    k_row_of<<<nblk(n), TB, 0, c->st>>>(n, DP<uint32_t>(c->id[from]), row_of);
+    Arr8<R> a = {{DP<R>(c->x[from]), DP<R>(c->y[from]), DP<R>(c->z[from]), DP<R>(c->vx[from]), DP<R>(c->vy[from]),
+                  DP<R>(c->vz[from]), DP<R>(c->m[from]), DP<R>(c->q[from])}};
+    Arr8<R> b = {{DP<R>(c->x[k]), DP<R>(c->y[k]), DP<R>(c->z[k]), DP<R>(c->vx[k]), DP<R>(c->vy[k]), DP<R>(c->vz[k]),
+                  DP<R>(c->m[k]), DP<R>(c->q[k])}};
+    k_reorder<R><<<nblk(n), TB, 0, c->st>>>(n, DP<uint32_t>(c->id[k]), row_of, a, b);
+    NB_LAUNCHED(c, "replay reorder");
+    return NBODY_OK;
+}
+
+// time points 0 .. nsteps of the recorded run, each evaluated on its recorded tree and lists from
+// the given initial state
+int replay(nbody_ctx* c, const double* pos, const double* vel, const double* mass, const double* charge, int nsteps,
+           double* pos_out, double* vel_out) {
+    const int64_t n = c->n;
+    int from = 1 - c->cur;            // the initial state, input order, identity ids
+    NB_TRY(nb_upload_state(c, from, n, pos, vel, mass, charge, nullptr));
+    c->lists_frozen = true;
+    for (int pt = 0; pt <= nsteps; ++pt) {
+        int rc = NBODY_OK;
+        if (pt > 0) rc = nb_kick_drift(c);                               // in the previous order
+        if (rc == NBODY_OK) {
+            c->cur = 1 - from;
+            rc = rec_load(c, pt);                                        // tree, lists and plan of pt
+        }
+        if (rc == NBODY_OK) rc = c->rsz == 4 ? reorder_t<float>(c, from) : reorder_t<double>(c, from);
+        if (rc == NBODY_OK) rc = nb_evaluate_frozen(c, pt == 0 ? NB_INTEG_NONE : NB_INTEG_KDK_CLOSE);
+        if (rc != NBODY_OK) {
+            c->lists_frozen = false;
+            return rc;
+        }
+        from = c->cur;
+    }
+    c->lists_frozen = false;
+    NB_TRY(nb_download_state(c, 1));
+    const double* st = DP<double>(c->stage);
+    if (pos_out) NB_CU(c, cudaMemcpyAsync(pos_out, st, sizeof(double) * 3 * n, cudaMemcpyDefault, c->st));
+    if (vel_out) NB_CU(c, cudaMemcpyAsync(vel_out, st + 3 * n, sizeof(double) * 3 * n, cudaMemcpyDefault, c->st));
+    NB_CU(c, cudaStreamSynchronize(c->st));
+    return NBODY_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nbody_forward_replay(nbody_ctx* c, const double* pos, const double* vel, const double* mass,
+                         const double* charge, int nsteps, double* pos_out, double* vel_out) {
+    if (!c || !pos || !mass) return NBODY_ERR_INVALID;
+    if (c->ck_steps < 1 || !c->rec_mode)
+        return nb_fail(c, NBODY_ERR_STATE, "no run recorded with every evaluation (nbody_forward_checkpointed, every = 0)");
+    if (nsteps < 0) nsteps = c->ck_steps;
+    if (nsteps > c->ck_steps) return nb_fail(c, NBODY_ERR_INVALID, "nsteps exceeds the recorded steps");
+    NB_CU(c, cudaSetDevice(c->device));
+    const int rc = replay(c, pos, vel, mass, charge, nsteps, pos_out, vel_out);
+    // back to the recorded run's final state with its evaluation current, replay or not
+    NB_TRY(snap_load(c, final_slot(c)));
+    NB_TRY(rec_load(c, c->ck_steps));
+    c->eval_current = true;
+    c->tree_at_final = true;
+    NB_CU(c, cudaStreamSynchronize(c->st));
+    return rc;
 }
 
 int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* gx0, double* gv0, double* gq,

@@ -491,6 +491,8 @@ int force_vjp(nbody_ctx* c, double coef) {
         B.nnodes = nn;
         B.info = DP<int32_t>(c->info);
         B.wait_cycles = c->copy_cycles;
+        NB_TRY((dtab_ensure<MODE, P>(c)));
+        dtab_args<MODE, P>(c, B);
         constexpr int W = M2LSmem<MODE, P>::warps;
         const size_t smem = (size_t)W * M2LSmem<MODE, P>::per_warp;
         NB_CU(c, cudaFuncSetAttribute(k_m2l<MODE, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -275,6 +275,19 @@ int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
     return NBODY_OK;
 }
 
+// the far and near field (with the integrator epilogue) on the tree and lists already loaded
+// (lists_frozen set): no kick, re-sort, tree or list building
+int nb_evaluate_frozen(nbody_ctx* c, int integ) {
+    c->launches = 0;
+    c->eval_current = false;
+    NB_CU(c, cudaMemsetAsync(c->info.p, 0, sizeof(int32_t), c->st));   // INFO_ERR
+    NB_TRY(fmm(c, integ, false));
+    NB_CU(c, cudaMemcpyAsync(c->h_info, c->info.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->st));
+    NB_CU(c, cudaStreamSynchronize(c->st));
+    NB_TRY(nb_check_async(c));
+    return NBODY_OK;
+}
+
 // the adaptive dt from the last evaluation's largest acceleration (nbody_set_timestep_control)
 static double adaptive_dt(const nbody_ctx* c) {
     const double len = c->dt_len > 0.0 ? c->dt_len : c->prm.eps;
@@ -303,6 +316,38 @@ int diag_t(nbody_ctx* c, double* out) {
 }
 
 }  // namespace
+
+// arrays in input order (host or device memory) -> state buffer k with identity ids (the state
+// buffers and the staging area must already hold n particles)
+int nb_upload_state(nbody_ctx* c, int k, int64_t n, const double* pos, const double* vel, const double* mass,
+                    const double* charge, const double* acc) {
+    double* st = DP<double>(c->stage);
+    NB_CU(c, cudaMemcpyAsync(st, pos, sizeof(double) * 3 * n, cudaMemcpyDefault, c->st));
+    if (vel) NB_CU(c, cudaMemcpyAsync(st + 3 * n, vel, sizeof(double) * 3 * n, cudaMemcpyDefault, c->st));
+    else NB_CU(c, cudaMemsetAsync(st + 3 * n, 0, sizeof(double) * 3 * n, c->st));
+    NB_CU(c, cudaMemcpyAsync(st + 6 * n, mass, sizeof(double) * n, cudaMemcpyDefault, c->st));
+    if (charge) NB_CU(c, cudaMemcpyAsync(st + 7 * n, charge, sizeof(double) * n, cudaMemcpyDefault, c->st));
+    if (acc) NB_CU(c, cudaMemcpyAsync(st + 9 * n, acc, sizeof(double) * 3 * n, cudaMemcpyDefault, c->st));
+    if (c->rsz == 4)
+        k_upload<float><<<nblk(n), TB, 0, c->st>>>(n, st, DP<float>(c->x[k]), DP<float>(c->y[k]), DP<float>(c->z[k]),
+                                                   DP<float>(c->vx[k]), DP<float>(c->vy[k]), DP<float>(c->vz[k]),
+                                                   DP<float>(c->ax[k]), DP<float>(c->ay[k]), DP<float>(c->az[k]),
+                                                   DP<float>(c->m[k]), DP<float>(c->q[k]), DP<uint32_t>(c->id[k]),
+                                                   charge != nullptr, acc != nullptr);
+    else
+        k_upload<double><<<nblk(n), TB, 0, c->st>>>(n, st, DP<double>(c->x[k]), DP<double>(c->y[k]),
+                                                    DP<double>(c->z[k]), DP<double>(c->vx[k]), DP<double>(c->vy[k]),
+                                                    DP<double>(c->vz[k]), DP<double>(c->ax[k]), DP<double>(c->ay[k]),
+                                                    DP<double>(c->az[k]), DP<double>(c->m[k]), DP<double>(c->q[k]),
+                                                    DP<uint32_t>(c->id[k]), charge != nullptr, acc != nullptr);
+    NB_LAUNCHED(c, "upload");
+    return NBODY_OK;
+}
+
+// the current state buffer -> the staging area, input order (order = 1) or sorted (0)
+int nb_download_state(nbody_ctx* c, int order) {
+    return c->rsz == 4 ? download_t<float>(c, order) : download_t<double>(c, order);
+}
 
 extern "C" {
 
@@ -359,6 +404,7 @@ int nbody_create(const nbody_params* p, nbody_ctx** out) {
         if ((rc = nb_grow(c, c->box, sizeof(BoxDev)))) break;
         if ((rc = nb_grow(c, c->bbox, 6 * sizeof(unsigned long long)))) break;
         if ((rc = nb_cuda(c, cudaMallocHost(&c->h_info, sizeof(int32_t) * INFO_WORDS), "cudaMallocHost"))) break;
+        if ((rc = nb_cuda(c, cudaMallocHost(&c->h_box, sizeof(BoxDev)), "cudaMallocHost"))) break;
         if ((rc = nb_cuda(c, cudaMemsetAsync(c->info.p, 0, sizeof(int32_t) * INFO_WORDS, c->st), "memset"))) break;
         for (int i = 0; i < 14 && !rc; ++i) rc = nb_cuda(c, cudaEventCreate(&c->ev[i]), "cudaEventCreate");
         for (int i = 0; i < NB_P2P_CLASSES && !rc; ++i) {
@@ -393,10 +439,11 @@ int nbody_destroy(nbody_ctx* c) {
                       &c->adj_gq, &c->adj_gm, &c->adj_nu, &c->adj_lamL, &c->adj_lamM, &c->adj_near,
                       &c->snaps, &c->lst_seg, &c->lst_nch, &c->lst_first, &c->lst_target, &c->lst_cnt,
                       &c->lst_off, &c->lst_cp, &c->lst_rows, &c->cls_key[0], &c->cls_key[1], &c->cls_val[0], &c->cls_val[1],
-                      &c->leaves_tmp, &c->wait_probe})
+                      &c->leaves_tmp, &c->wait_probe, &c->dtab})
         release(*b);
     for (EvalRecord& r : c->recs) release(r.buf);
     if (c->h_info) cudaFreeHost(c->h_info);
+    if (c->h_box) cudaFreeHost(c->h_box);
     if (c->h_amax) cudaFreeHost(c->h_amax);
     release(c->amax);
     for (int i = 0; i < 16; ++i)
@@ -425,27 +472,7 @@ int nbody_set_state(nbody_ctx* c, int64_t n, const double* pos, const double* ve
     c->eval_current = false;
     c->cur = 0;
     NB_TRY(alloc_state(c, n));
-    double* st = DP<double>(c->stage);
-    NB_CU(c, cudaMemcpyAsync(st, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->st));
-    if (vel) NB_CU(c, cudaMemcpyAsync(st + 3 * n, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->st));
-    else NB_CU(c, cudaMemsetAsync(st + 3 * n, 0, sizeof(double) * 3 * n, c->st));
-    NB_CU(c, cudaMemcpyAsync(st + 6 * n, mass, sizeof(double) * n, cudaMemcpyHostToDevice, c->st));
-    if (charge) NB_CU(c, cudaMemcpyAsync(st + 7 * n, charge, sizeof(double) * n, cudaMemcpyHostToDevice, c->st));
-    if (acc) NB_CU(c, cudaMemcpyAsync(st + 9 * n, acc, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->st));
-    const int k = 0;
-    if (c->rsz == 4)
-        k_upload<float><<<nblk(n), TB, 0, c->st>>>(n, st, DP<float>(c->x[k]), DP<float>(c->y[k]), DP<float>(c->z[k]),
-                                                   DP<float>(c->vx[k]), DP<float>(c->vy[k]), DP<float>(c->vz[k]),
-                                                   DP<float>(c->ax[k]), DP<float>(c->ay[k]), DP<float>(c->az[k]),
-                                                   DP<float>(c->m[k]), DP<float>(c->q[k]), DP<uint32_t>(c->id[k]),
-                                                   charge != nullptr, acc != nullptr);
-    else
-        k_upload<double><<<nblk(n), TB, 0, c->st>>>(n, st, DP<double>(c->x[k]), DP<double>(c->y[k]),
-                                                    DP<double>(c->z[k]), DP<double>(c->vx[k]), DP<double>(c->vy[k]),
-                                                    DP<double>(c->vz[k]), DP<double>(c->ax[k]), DP<double>(c->ay[k]),
-                                                    DP<double>(c->az[k]), DP<double>(c->m[k]), DP<double>(c->q[k]),
-                                                    DP<uint32_t>(c->id[k]), charge != nullptr, acc != nullptr);
-    NB_LAUNCHED(c, "upload");
+    NB_TRY(nb_upload_state(c, 0, n, pos, vel, mass, charge, acc));
     NB_CU(c, cudaStreamSynchronize(c->st));
     c->n = n;
     c->escapes = 0;

@@ -21,6 +21,8 @@
 // reproducible run to run.
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <type_traits>
 
 #include "nbody_internal.cuh"
@@ -295,7 +297,97 @@ struct M2LArgs {
     double eps2;
     int64_t nnodes;
     long long wait_cycles;   // bound of each wait for this warp's bulk copies (SM clock cycles)
+    const void* dtab;        // S*: derivative table (FP64 form; rows of stride nb_tm<P>), null: none
+    int dt_R, dt_levels;     // its offset range and levels
 };
+
+// ---------------------------------------------------------------------------
+// far field, part 1b (FP64 form): the derivative tensor D(r) of the M2L operator, tabulated.  Two
+// cells of one level are an integer number of cells apart, and cells one level apart an odd number
+// of half cells of the finer level, so at a given root box the pairs of the far-field lists take
+// few distinct displacements (at theta = 0.5: same-level offsets within +-7 cells).  Per level l
+// the table holds, in rows of nb_tm<P> entries:
+//   [0, W^3)              t and s at level l, cell offset o = i_t - i_s in [-R, R]^3   (W = 2R+1)
+//   [W^3, W^3 + V^3)      t at l, s at l+1, half-cell offset h = 2(2 i_t + 1) - (2 i_s + 1)
+//   [W^3 + V^3, W^3+2V^3) t at l+1, s at l, h = (2 i_t + 1) - 2(2 i_s + 1)
+//                         (h odd, |h| <= 2R+1: V = 2R+2 values per axis)
+// Each row is derivs() of the same exact displacement (fine units x fine unit) that the M2L kernel
+// forms for such a pair.  Pairs outside the table (cells two or more levels apart, offsets beyond
+// R) compute D in place.  The FP64 form's D costs ~300 FP64 operations per pair at 1/64 of the
+// FP32 rate, so a 448-byte row from L2 is cheaper; the FP32 bulk forms compute D per pair (a table
+// row is one more stream from L2 beside the multipole rows, which measured slower there).
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ int dtab_rows_per_level(int R) {
+    const int W = 2 * R + 1, V = 2 * R + 2;
+    return W * W * W + 2 * V * V * V;
+}
+
+// row of the pair (target t, source s), or -1
+__device__ __forceinline__ int dtab_row(const NodeRec& t, const NodeRec& s, int R, int levels) {
+    const int lt = t.level, ls = s.level;
+    const int W = 2 * R + 1, V = 2 * R + 2, Q = dtab_rows_per_level(R);
+    if (lt == ls) {
+        if (lt >= levels) return -1;
+        const int ox = (int)t.ix - (int)s.ix, oy = (int)t.iy - (int)s.iy, oz = (int)t.iz - (int)s.iz;
+        if (ox < -R || ox > R || oy < -R || oy > R || oz < -R || oz > R) return -1;
+        return lt * Q + ((ox + R) * W + (oy + R)) * W + (oz + R);
+    }
+    int hx, hy, hz, l, blk;
+    if (ls == lt + 1) {
+        hx = 2 * (2 * (int)t.ix + 1) - (2 * (int)s.ix + 1);
+        hy = 2 * (2 * (int)t.iy + 1) - (2 * (int)s.iy + 1);
+        hz = 2 * (2 * (int)t.iz + 1) - (2 * (int)s.iz + 1);
+        l = lt;
+        blk = W * W * W;
+    } else if (lt == ls + 1) {
+        hx = (2 * (int)t.ix + 1) - 2 * (2 * (int)s.ix + 1);
+        hy = (2 * (int)t.iy + 1) - 2 * (2 * (int)s.iy + 1);
+        hz = (2 * (int)t.iz + 1) - 2 * (2 * (int)s.iz + 1);
+        l = ls;
+        blk = W * W * W + V * V * V;
+    } else {
+        return -1;
+    }
+    const int H = 2 * R + 1;
+    if (l + 1 >= levels || hx < -H || hx > H || hy < -H || hy > H || hz < -H || hz > H) return -1;
+    return l * Q + blk + (((hx + H) >> 1) * V + ((hy + H) >> 1)) * V + ((hz + H) >> 1);
+}
+
+template <typename S, int P>
+__global__ void __launch_bounds__(128) k_dtab(int levels, int R, const BoxDev* __restrict__ boxp, double eps2d,
+                                              S* __restrict__ tab) {
+    constexpr int T = nb_terms<P>::value;
+    constexpr int TM = nb_tm<P>::value;
+    const int Q = dtab_rows_per_level(R);
+    const int64_t row = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    if (row >= (int64_t)levels * Q) return;
+    const int l = (int)(row / Q), j = (int)(row % Q);
+    const int W = 2 * R + 1, V = 2 * R + 2, H = 2 * R + 1;
+    int fx, fy, fz;                  // displacement t - s in fine units (side / 2^22)
+    bool used = true;
+    if (j < W * W * W) {
+        const int ox = j / (W * W) - R, oy = (j / W) % W - R, oz = j % W - R;
+        const int u = 1 << (NB_LEVELS + 1 - l);
+        fx = ox * u; fy = oy * u; fz = oz * u;
+    } else {
+        const int k = (j - W * W * W) % (V * V * V);
+        const int hx = 2 * (k / (V * V)) - H, hy = 2 * ((k / V) % V) - H, hz = 2 * (k % V) - H;
+        used = l + 1 <= NB_LEVELS;
+        const int u = used ? 1 << (NB_LEVELS - 1 - l) : 0;
+        fx = hx * u; fy = hy * u; fz = hz * u;
+    }
+    S* out = tab + row * TM;
+    if (!used) {
+        for (int a = 0; a < TM; ++a) out[a] = S(0);
+        return;
+    }
+    const S unit = (S)boxp->unit;
+    const S dx = (S)fx * unit, dy = (S)fy * unit, dz = (S)fz * unit;
+    S D[T];
+    Ops<S, P>::template derivs<1>(dx, dy, dz, (S)eps2d, D);
+    for (int a = 0; a < T; ++a) out[a] = D[a];
+    for (int a = T; a < TM; ++a) out[a] = S(0);
+}
 
 template <int MODE, int P>
 struct M2LSmem {
@@ -372,6 +464,7 @@ __global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A)
     const S unit = (S)A.box->unit;
     const S eps2 = (S)A.eps2;
     const S* Msrc = (const S*)A.Mm2l;
+    const S* __restrict__ dtab = (const S*)A.dtab;
     const uint32_t off = A.m2l_off[t], cnt = A.m2l_cnt[t];
     const uint32_t nbatch = (cnt + 31) / 32;
     S Lreg[LS ? 1 : T];
@@ -424,7 +517,13 @@ __global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A)
             const S dx = (S)(tcx - sx) * unit, dy = (S)(tcy - sy) * unit, dz = (S)(tcz - sz) * unit;
             const S* row = rows + (k * 32 + lane) * SST;
             if constexpr (LS) {
-                Ops<S, P>::template derivs<32>(dx, dy, dz, eps2, laneD + lane);
+                const int drow = dtab ? dtab_row(nt, sn, A.dt_R, A.dt_levels) : -1;
+                if (drow >= 0) {
+                    const S* dr = dtab + (int64_t)drow * TM;
+                    for (int a = 0; a < T; ++a) laneD[a * 32 + lane] = dr[a];
+                } else {
+                    Ops<S, P>::template derivs<32>(dx, dy, dz, eps2, laneD + lane);
+                }
                 Ops<S, P>::template m2l_v<32>(row, laneD + lane, laneL + lane);
             } else {
                 S D[T];
@@ -855,6 +954,43 @@ int p2p_launch_classes(nbody_ctx* c, const P2PArgs& B) {
     NB_TRY(one(std::integral_constant<int, 0>()));
     return nb_join(c);
 }
+// (re)builds the FP64 form's derivative table when the root box side, the softening, the opening
+// angle's offset range or the order changed, or the tree is deeper than the table
+template <int MODE, int P>
+int dtab_ensure(nbody_ctx* c) {
+    typedef typename Prec<MODE>::S S;
+    if (!Prec<MODE>::lane_smem) return NBODY_OK;   // the FP32 bulk forms compute D per pair
+    const int R = (int)std::floor(2.0 * std::sqrt(3.0) / c->prm.theta) + 1;
+    const int levels = c->depth + 1;
+    if (R > 24) return NBODY_OK;        // small opening angles: too many offsets, D is computed per pair
+    if (c->dt_prec == MODE && c->dt_order == P && c->dt_R == R && c->dt_side == c->box_side &&
+        c->dt_eps == c->prm.eps && c->dt_levels >= levels)
+        return NBODY_OK;
+    const int lv = std::max(levels, c->dt_prec == MODE && c->dt_order == P && c->dt_R == R ? c->dt_levels : 0);
+    const int64_t rows = (int64_t)lv * dtab_rows_per_level(R);
+    NB_TRY(nb_grow(c, c->dtab, sizeof(S) * nb_tm<P>::value * (size_t)rows));
+    k_dtab<S, P><<<(unsigned)((rows + 127) / 128), 128, 0, c->st>>>(lv, R, DP<BoxDev>(c->box),
+                                                                    c->prm.eps * c->prm.eps, DP<S>(c->dtab));
+    NB_LAUNCHED(c, "m2l derivative table");
+    c->launches += 1;
+    c->dt_prec = MODE;
+    c->dt_order = P;
+    c->dt_R = R;
+    c->dt_side = c->box_side;
+    c->dt_eps = c->prm.eps;
+    c->dt_levels = lv;
+    return NBODY_OK;
+}
+
+template <int MODE, int P>
+void dtab_args(const nbody_ctx* c, M2LArgs& B) {
+    const bool ok = Prec<MODE>::lane_smem && c->dt_prec == MODE && c->dt_order == P && c->dt_side == c->box_side &&
+                    c->dt_eps == c->prm.eps;
+    B.dtab = ok ? c->dtab.p : nullptr;
+    B.dt_R = c->dt_R;
+    B.dt_levels = ok ? c->dt_levels : 0;
+}
+
 template <int MODE, int P>
 int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     typedef typename Prec<MODE>::R R;
@@ -886,7 +1022,7 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     }
     if (c->timing) cudaEventRecord(c->ev[4], c->st);
 
-    NB_TRY(nb_build_lists(c));
+    if (!c->lists_frozen) NB_TRY(nb_build_lists(c));
     if (c->timing) cudaEventRecord(c->ev[5], c->st);
     {
         M2LArgs B;
@@ -900,6 +1036,8 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
         B.nnodes = nn;
         B.info = DP<int32_t>(c->info);
         B.wait_cycles = c->copy_cycles;
+        NB_TRY((dtab_ensure<MODE, P>(c)));
+        dtab_args<MODE, P>(c, B);
         constexpr int W = M2LSmem<MODE, P>::warps;
         const size_t smem = (size_t)W * M2LSmem<MODE, P>::per_warp;
         NB_CU(c, cudaFuncSetAttribute(k_m2l<MODE, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -98,6 +98,7 @@ struct EvalRecord {
     DevBuf buf;
     int64_t nn = 0, nl = 0;
     int depth = 0;
+    double box_side = 0.0;         // root box side of that evaluation
     int level_start[NB_LEVELS + 3] = {0};
     int32_t info[INFO_WORDS] = {0};
 };
@@ -154,7 +155,15 @@ struct nbody_ctx {
     // small device blocks + pinned mirrors
     DevBuf info, box, bbox;
     int32_t* h_info = nullptr;
-    double* h_box = nullptr;
+    BoxDev* h_box = nullptr;       // root box of the current tree, read at the tree's synchronisation
+    double box_side = 0.0;         // its side (the FP64 form's M2L derivative table depends on it)
+
+    // M2L derivative table of the FP64 form: D(r) of every same-level cell offset within +-dt_R and
+    // every offset of cells one level apart (odd half-cell offsets within +-(2 dt_R + 1)), levels
+    // 0 .. dt_levels - 1
+    DevBuf dtab;
+    int dt_R = 0, dt_levels = 0, dt_order = 0, dt_prec = -1;
+    double dt_side = 0.0, dt_eps = -1.0;
 
     // adjoint (input-order accumulators, adjoint expansions, trajectory snapshots)
     DevBuf adj_lx, adj_lv, adj_gq, adj_gm, adj_nu, adj_lamL, adj_lamM, adj_near;
@@ -166,6 +175,7 @@ struct nbody_ctx {
     bool tree_at_final = false;    // the last evaluation was the recorded run's final one
     bool rec_mode = false;         // the recorded run kept every evaluation (no re-evaluation backward)
     bool eval_current = false;     // tree, lists and expansions match the current state
+    bool lists_frozen = false;     // the force evaluation reuses the loaded lists (frozen-structure replay)
     std::vector<EvalRecord> recs;  // its evaluations, time points 0 .. steps
 
     // per-phase timing
@@ -226,7 +236,14 @@ int nb_check_async(nbody_ctx* c);
 int nb_radix_sort(nbody_ctx* c, int64_t n, uint64_t* k0, uint32_t* v0, uint64_t* k1, uint32_t* v1, int begin_bit,
                   int end_bit, int* result_in_first);
 
+// state upload (input order, identity ids) into buffer k, and download of the current buffer into
+// the staging area (api.cu)
+int nb_upload_state(nbody_ctx* c, int k, int64_t n, const double* pos, const double* vel, const double* mass,
+                    const double* charge, const double* acc);
+int nb_download_state(nbody_ctx* c, int order);
+
 // tree (tree.cu)
+int nb_kick_drift(nbody_ctx* c);
 int nb_begin_step(nbody_ctx* c, int kdk);
 int nb_sort_and_gather(nbody_ctx* c);
 int nb_build_tree(nbody_ctx* c);
@@ -245,6 +262,8 @@ int nb_traj_close(nbody_ctx* c);
 
 // one force evaluation at the current positions (api.cu); kdk = 1 applies the opening kick and drift first
 int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot);
+// the far and near field only, on the tree and lists already loaded (lists_frozen) (api.cu)
+int nb_evaluate_frozen(nbody_ctx* c, int integ);
 
 // fmm (fmm_*.cu)
 int nb_fmm_forces_fp32(nbody_ctx* c, int integ, bool want_pot);

@@ -397,6 +397,22 @@ int nb_begin_step(nbody_ctx* c, int kdk) {
     return c->rsz == 4 ? begin_step_t<float>(c, kdk) : begin_step_t<double>(c, kdk);
 }
 
+// opening kick + drift of the current state buffer, nothing else (the frozen-structure replay)
+int nb_kick_drift(nbody_ctx* c) {
+    unsigned g = nblk(c->n);
+    if (g > 152 * 8) g = 152 * 8;
+    if (g == 0) g = 1;
+    unsigned long long* bb = DP<unsigned long long>(c->bbox);
+    if (c->rsz == 4)
+        k_kick_drift_bbox<float><<<g, TB, 0, c->st>>>(c->n, state<float>(c, c->cur), 0.5 * c->prm.dt, c->prm.dt, 1,
+                                                      bb, DP<int32_t>(c->info));
+    else
+        k_kick_drift_bbox<double><<<g, TB, 0, c->st>>>(c->n, state<double>(c, c->cur), 0.5 * c->prm.dt, c->prm.dt,
+                                                       1, bb, DP<int32_t>(c->info));
+    NB_LAUNCHED(c, "kick_drift");
+    return NBODY_OK;
+}
+
 int nb_sort_and_gather(nbody_ctx* c) {
     int first = 1;
     NB_TRY(nb_radix_sort(c, c->n, DP<uint64_t>(c->keys[0]), DP<uint32_t>(c->vals[0]), DP<uint64_t>(c->keys[1]),
@@ -420,7 +436,9 @@ int nb_build_tree(nbody_ctx* c) {
     c->launches += 2;
     NB_TRY(nb_scan_u32(c, DP<uint32_t>(c->nc), DP<uint32_t>(c->pfx), n, (uint32_t*)(info + INFO_NNODES)));
     NB_CU(c, cudaMemcpyAsync(c->h_info, info, sizeof(int32_t) * INFO_WORDS, cudaMemcpyDeviceToHost, c->st));
+    NB_CU(c, cudaMemcpyAsync(c->h_box, c->box.p, sizeof(BoxDev), cudaMemcpyDeviceToHost, c->st));
     NB_CU(c, cudaStreamSynchronize(c->st));
+    c->box_side = c->h_box->side;
     if (c->h_info[INFO_SCAN_ERR]) return nb_fail(c, NBODY_ERR_CUDA, "a device scan did not complete in time");
     const uint32_t err = (uint32_t)c->h_info[INFO_ERR];
     if (err & NB_ERRBIT_NONFINITE) return nb_fail(c, NBODY_ERR_STATE, "non-finite particle position");

@@ -227,6 +227,21 @@ class CudaSimulation:
                                                   ptr(gm)))
         return gx0, gv0, gq, gm
 
+    def replay(self, pos, vel=None, mass=None, charge=None, steps=None):
+        """Frozen-structure replay of the run recorded with forward_checkpointed(steps, 0): from this
+        initial state (input order), `steps` leapfrog steps whose evaluations reuse the recorded trees,
+        lists and near-field plans.  Returns the final (pos, vel) in input order; the context keeps
+        the recorded run."""
+        n = self.n
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(n, 3)
+        vel = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(n, 3)
+        mass = np.ones(n) if mass is None else np.ascontiguousarray(mass, dtype=np.float64).reshape(n)
+        charge = None if charge is None else np.ascontiguousarray(charge, dtype=np.float64).reshape(n)
+        po, vo = np.empty((n, 3)), np.empty((n, 3))
+        check(self._h, _lib.load().nbody_forward_replay(self._h, ptr(pos), ptr(vel), ptr(mass), ptr(charge),
+                                                        -1 if steps is None else int(steps), ptr(po), ptr(vo)))
+        return po, vo
+
     def trajectory_open(self, path, every: int = 1, order: str = "leaf", digits: int = 6):
         """Append a CSV row (time, x, y, z of every particle) every `every` steps, as the reference's
         main loop writes particles.csv; order 'leaf' (the reference's) or 'input'."""
