@@ -159,11 +159,13 @@ int nbody_force_vjp(nbody_ctx* c, const double* mu, double* gx, double* gq, doub
 /* Advances nsteps leapfrog (KDK) steps like nbody_step, recording for
    nbody_backward.
    every >= 1: the sorted state every `every` steps (plus the final state):
-   (ceil(nsteps / every) + every) snapshots of about 92 bytes per particle in
-   the FP64 and mixed forms, 48 in FP32.  The reverse sweep re-evaluates each
-   time point's tree and far field from its snapshot (the near field is not
-   needed: snapshots hold the accelerations); with every > 1 it also
-   recomputes the every - 1 full steps inside each checkpoint interval.
+   (ceil(nsteps / every) + 1) snapshots of about 92 bytes per particle in
+   the FP64 and mixed forms, 48 in FP32.  The reverse sweep recomputes each
+   checkpoint interval forward from its snapshot (the checkpoint's far field
+   only: the snapshot holds its accelerations; then every - 1 full steps) and
+   records those evaluations whole, so it holds the records of one interval
+   (about 370 bytes per particle per time point at order 5 and leaf capacity
+   64) while it runs.
    every = 0: every time point's whole evaluation (tree, lists, local
    expansions, particle offsets), so the reverse sweep evaluates nothing:
    about 370 bytes per particle per time point at order 5 and leaf capacity
@@ -314,6 +316,14 @@ int nbody_set_wait_limits(nbody_ctx* c, int64_t scan_polls, int64_t copy_cycles)
      copy delivers (context's copy_cycles limit): NBODY_ERR_CUDA "a far-field
      copy did not complete in time"; the context stays usable. */
 int nbody_selftest_wait(nbody_ctx* c, int which);
+
+/* 1 in the NBODY_DEBUG_BOUNDS build of the library (libnbody_gb300_debug.so),
+   0 otherwise.  That build checks every index read from device data (sorted
+   order, node ids of the interaction lists, particle ranges): an index out
+   of range is replaced by an in-bounds one and the failing site is reported
+   as NBODY_ERR_CUDA at the end of the evaluation, so a bug shows as an error
+   instead of a fault.  (No counterpart in the reference.) */
+int nbody_debug_bounds(void);
 
 /* Simulated time. */
 int nbody_get_time(nbody_ctx* c, double* t);

@@ -30,7 +30,7 @@ EXPORTS = ("nbody_default_params", "nbody_create", "nbody_destroy", "nbody_set_s
            "nbody_measure_peaks", "nbody_direct_forces_static", "nbody_force_vjp", "nbody_forward_checkpointed",
            "nbody_backward", "nbody_device_memory", "nbody_trajectory_open", "nbody_trajectory_close",
            "nbody_set_timestep_control", "nbody_last_timestep", "nbody_set_escape_policy", "nbody_set_wait_limits",
-           "nbody_selftest_wait", "nbody_forward_replay")
+           "nbody_selftest_wait", "nbody_forward_replay", "nbody_debug_bounds")
 
 
 class Params(C.Structure):
@@ -56,7 +56,7 @@ def load(path: str | None = None):
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("NBODY_LIB_PATH") or LIB_PATH
     if not os.path.exists(path):
         raise ImportError(f"{path} is missing: build it with `python -m nbody_gb300.build`")
     L = C.CDLL(path)
@@ -100,6 +100,7 @@ def load(path: str | None = None):
     L.nbody_set_wait_limits.argtypes = [vp, C.c_int64, C.c_int64]
     L.nbody_selftest_wait.argtypes = [vp, C.c_int]
     L.nbody_forward_replay.argtypes = [vp, vp, vp, vp, vp, C.c_int, vp, vp]
+    L.nbody_debug_bounds.argtypes = []
     L.nbody_last_error.argtypes = [vp]
     L.nbody_last_error.restype = C.c_char_p
     for name in EXPORTS:

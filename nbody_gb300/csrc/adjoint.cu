@@ -9,12 +9,14 @@
 //   its VJP is taken with mu = c lambda_v and added to lambda_x, q and m;
 //   before time point pt < N the drift x_{pt+1} = x_pt + dt v gives
 //   lambda_v += dt lambda_x.
-// The VJP at a time point needs its tree, lists and local expansions, so each
-// time point is re-evaluated from a snapshot, far field only: the snapshot
-// already holds that point's accelerations (the run's last point and the last
-// point of every recomputed segment are current without re-evaluation).
-// Snapshots hold the sorted state (positions, velocities, accelerations,
-// masses, charges, ids), so a recomputed segment is bitwise the recorded one.
+// The VJP at a time point needs its tree, lists and local expansions.  With
+// checkpoints, each segment is recomputed forward from its checkpoint (whose
+// snapshot already holds the accelerations: its far field only is evaluated)
+// and every evaluation of the segment is recorded whole, so the segment's
+// reverse pass re-evaluates nothing; memory: one snapshot per checkpoint plus
+// the records of one segment.  Snapshots hold the sorted state (positions,
+// velocities, accelerations, masses, charges, ids), so a recomputed segment
+// is bitwise the recorded one.
 #include <algorithm>
 
 #include "nbody_internal.cuh"
@@ -235,10 +237,9 @@ int rec_load(nbody_ctx* c, int j) {
     return NBODY_OK;
 }
 
-// snapshot slots: 0 .. nck-1 checkpoints, then `every - 1` segment slots, then the final state
+// snapshot slots: 0 .. nck-1 checkpoints, then the final state
 int nck(const nbody_ctx* c) { return c->rec_mode ? 0 : (c->ck_steps + c->ck_every - 1) / c->ck_every; }
-int seg_slot(const nbody_ctx* c, int j) { return nck(c) + j; }
-int final_slot(const nbody_ctx* c) { return c->rec_mode ? 0 : nck(c) + c->ck_every - 1; }
+int final_slot(const nbody_ctx* c) { return nck(c); }
 
 }  // namespace
 
@@ -263,6 +264,7 @@ int nbody_force_vjp(nbody_ctx* c, const double* mu, double* gx, double* gq, doub
     NB_TRY(download_r(c, c->adj_gq, n, gq, st + 3 * n));
     NB_TRY(download_r(c, c->adj_gm, n, gm, st + 4 * n));
     NB_CU(c, cudaStreamSynchronize(c->st));
+    NB_TRY(nb_dbg_check(c));
     c->launches = c->launches - l0;
     if (c->timing)
         for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&c->phase_ms[7 + i], c->ev[8 + i], c->ev[9 + i]);
@@ -283,7 +285,7 @@ int nbody_forward_checkpointed(nbody_ctx* c, int nsteps, int every, double* t_ou
     c->ck_steps = 0;
     c->rec_mode = rec;
     c->snap_bytes = snapshot_bytes(c);
-    const int slots = rec ? 1 : (nsteps + every - 1) / every + every;
+    const int slots = rec ? 1 : (nsteps + every - 1) / every + 1;
     NB_TRY(nb_grow(c, c->snaps, c->snap_bytes * (size_t)slots));
     // time point 0 needs its accelerations, and in record mode its whole evaluation
     if (!c->have_acc || (rec && !c->eval_current)) {
@@ -415,7 +417,7 @@ int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* g
         c->tree_at_final = true;
         c->time = c->ck_t0 + N * dt;
         NB_CU(c, cudaStreamSynchronize(c->st));
-        return NBODY_OK;
+        return nb_dbg_check(c);
     }
     // time point N
     if (!c->tree_at_final) {
@@ -423,23 +425,22 @@ int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* g
         NB_TRY(nb_evaluate(c, 0, NB_INTEG_FAR_ONLY, false));
     }
     NB_TRY(vjp(c, 0.5 * dt));
-    // segments [s0, e), last first
+    // segments [s0, e), last first: the checkpoint's tree, lists and far field (its snapshot holds
+    // the accelerations), then the recomputed steps s0+1 .. e-1, each evaluation recorded whole, so
+    // the segment's reverse pass re-evaluates nothing
     for (int s0 = ((N - 1) / every) * every; s0 >= 0; s0 -= every) {
         const int e = std::min(s0 + every, N);
         NB_TRY(snap_load(c, s0 / every));
         c->time = c->ck_t0 + s0 * dt;
-        for (int pt = s0 + 1; pt <= e - 1; ++pt) {       // recompute x_{s0+1} .. x_{e-1}
+        NB_TRY(nb_evaluate(c, 0, NB_INTEG_FAR_ONLY, false));
+        NB_TRY(rec_save(c, 0));
+        for (int pt = s0 + 1; pt <= e - 1; ++pt) {
             NB_TRY(nb_evaluate(c, 1, NB_INTEG_KDK_CLOSE, false));
-            if (pt < e - 1) NB_TRY(snap_save(c, seg_slot(c, pt - s0 - 1)));
+            NB_TRY(rec_save(c, pt - s0));
         }
         for (int pt = e - 1; pt >= s0; --pt) {
             NB_TRY(rev_drift(c));
-            if (pt < e - 1) {
-                NB_TRY(snap_load(c, pt == s0 ? s0 / every : seg_slot(c, pt - s0 - 1)));
-                NB_TRY(nb_evaluate(c, 0, NB_INTEG_FAR_ONLY, false));
-            } else if (e - 1 == s0) {
-                NB_TRY(nb_evaluate(c, 0, NB_INTEG_FAR_ONLY, false));
-            }
+            if (pt < e - 1) NB_TRY(rec_load(c, pt - s0));     // pt = e - 1 is the current evaluation
             NB_TRY(vjp(c, pt == 0 ? 0.5 * dt : dt));
         }
     }
@@ -451,7 +452,7 @@ int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* g
     NB_TRY(snap_load(c, final_slot(c)));
     c->time = c->ck_t0 + N * dt;
     NB_CU(c, cudaStreamSynchronize(c->st));
-    return NBODY_OK;
+    return nb_dbg_check(c);
 }
 
 }  // extern "C"

@@ -118,6 +118,7 @@ __global__ void __launch_bounds__(128) k_adj_l2pT(int64_t nleaves, const uint32_
 struct AdjP2PArgs {
     const uint32_t* leaves;
     int64_t nleaves;
+    int64_t nnodes, n;        // node and particle counts (index checks of the debug build)
     const NodeRec* nodes;
     const BoxDev* box;
     const void* src;          // S4* (offset from the leaf centre, q)
@@ -219,10 +220,10 @@ __device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE
             uint32_t my_s = 0, my_beg = 0, my_cnt = 0;
             S my_dx = 0, my_dy = 0, my_dz = 0;
             if ((uint32_t)lane < nbat) {
-                my_s = A.p2p_list[loff + base + lane];
+                my_s = NB_IDX(A.p2p_list[loff + base + lane], A.nnodes, NB_SITE_ADJ);
                 const NodeRec sn = A.nodes[my_s];
-                my_beg = sn.begin;
-                my_cnt = sn.count;
+                my_beg = NB_IDX(sn.begin, A.n, NB_SITE_ADJ);
+                my_cnt = NB_IDX(sn.count, A.n + 1 - my_beg, NB_SITE_ADJ);
                 disp_s<S>(sn, nt, unit, my_dx, my_dy, my_dz);
             }
             // partners of this batch in descending particle count (as in the forward near field)
@@ -426,6 +427,8 @@ int force_vjp(nbody_ctx* c, double coef) {
     // near field on the side streams (it needs only the seeds), far-field chain meanwhile on the main one
     AdjP2PArgs C;
     C.leaves = DP<uint32_t>(c->leaves);
+    C.nnodes = nn;
+    C.n = n;
     C.nleaves = nl;
     C.nodes = DP<NodeRec>(c->nodes);
     C.box = box;

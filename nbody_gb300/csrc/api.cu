@@ -237,6 +237,30 @@ int amax_t(nbody_ctx* c) {
 
 }  // namespace
 
+#ifdef NBODY_DEBUG_BOUNDS
+unsigned int nb_dbg_take_tree();
+unsigned int nb_dbg_take_sort();
+unsigned int nb_dbg_take_lists();
+unsigned int nb_dbg_take_fmm_fp32();
+unsigned int nb_dbg_take_fmm_mixed();
+unsigned int nb_dbg_take_fmm_fp64();
+#endif
+
+int nb_dbg_check(nbody_ctx* c) {
+#ifdef NBODY_DEBUG_BOUNDS
+    const unsigned int w = nb_dbg_take_tree() | nb_dbg_take_sort() | nb_dbg_take_lists() | nb_dbg_take_fmm_fp32() |
+                           nb_dbg_take_fmm_mixed() | nb_dbg_take_fmm_fp64();
+    if (w) {
+        char msg[96];
+        std::snprintf(msg, sizeof msg, "index check failed (debug build), site bits 0x%x", w);
+        return nb_fail(c, NBODY_ERR_CUDA, msg);
+    }
+#else
+    (void)c;
+#endif
+    return NBODY_OK;
+}
+
 int nb_check_async(nbody_ctx* c) {
     if ((uint32_t)c->h_info[INFO_ERR] & NB_ERRBIT_ASYNC)
         return nb_fail(c, NBODY_ERR_CUDA, "a far-field copy did not complete in time");
@@ -263,6 +287,7 @@ int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot) {
     NB_CU(c, cudaMemcpyAsync(c->h_info, c->info.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->st));
     NB_CU(c, cudaStreamSynchronize(c->st));
     NB_TRY(nb_check_async(c));
+    NB_TRY(nb_dbg_check(c));
     if (c->timing) {
         NB_CU(c, cudaEventSynchronize(c->ev[7]));
         for (int i = 0; i < 7; ++i) cudaEventElapsedTime(&c->phase_ms[i], c->ev[i], c->ev[i + 1]);
@@ -285,6 +310,7 @@ int nb_evaluate_frozen(nbody_ctx* c, int integ) {
     NB_CU(c, cudaMemcpyAsync(c->h_info, c->info.p, sizeof(int32_t), cudaMemcpyDeviceToHost, c->st));
     NB_CU(c, cudaStreamSynchronize(c->st));
     NB_TRY(nb_check_async(c));
+    NB_TRY(nb_dbg_check(c));
     return NBODY_OK;
 }
 
@@ -726,6 +752,14 @@ int nbody_get_time(nbody_ctx* c, double* t) {
     if (!c || !t) return NBODY_ERR_INVALID;
     *t = c->time;
     return NBODY_OK;
+}
+
+int nbody_debug_bounds(void) {
+#ifdef NBODY_DEBUG_BOUNDS
+    return 1;
+#else
+    return 0;
+#endif
 }
 
 const char* nbody_last_error(nbody_ctx* c) { return c ? c->err.c_str() : g_create_err.c_str(); }

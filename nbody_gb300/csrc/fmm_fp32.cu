@@ -43,3 +43,5 @@ int nb_copy_wait_selftest(nbody_ctx* c) {
     NB_CU(c, cudaStreamSynchronize(c->st));
     return nb_check_async(c);
 }
+
+NB_DBG_ACCESSOR(fmm_fp32)

@@ -8,3 +8,5 @@ int nb_fmm_forces_fp64(nbody_ctx* c, int integ, bool want_pot) {
 }
 
 int nb_fmm_vjp_fp64(nbody_ctx* c, double coef) { return nbfmm::vjp_dispatch<NBODY_PREC_FP64>(c, coef); }
+
+NB_DBG_ACCESSOR(fmm_fp64)

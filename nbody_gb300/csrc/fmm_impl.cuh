@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A)
     // this lane's list entry of batch b (0 past the end)
     auto entry = [&](uint32_t b) -> uint32_t {
         const uint32_t j = 32 * b + lane;
-        return b < nbatch && j < cnt ? A.m2l_list[off + j] : 0u;
+        return b < nbatch && j < cnt ? NB_IDX(A.m2l_list[off + j], A.nnodes, NB_SITE_M2L) : 0u;
     };
     // issue the bulk copies of batch b (source s of this lane, loaded one batch earlier) into stage
     // b & 1; returns the lane's source node record, loaded now and used one batch later
@@ -617,6 +617,7 @@ __global__ void __launch_bounds__(128) k_l2l(int lo, int hi, const NodeRec* __re
 struct P2PArgs {
     const uint32_t* leaves;
     int64_t nleaves;
+    int64_t nnodes, n;      // node and particle counts (index checks of the debug build)
     const NodeRec* nodes;
     const BoxDev* box;
     const void* src;        // S4*
@@ -744,10 +745,10 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
             uint32_t my_s = 0, my_beg = 0, my_cnt = 0;
             S my_dx = 0, my_dy = 0, my_dz = 0;
             if ((uint32_t)lane < nb) {
-                my_s = A.p2p_list[loff + base + lane];
+                my_s = NB_IDX(A.p2p_list[loff + base + lane], A.nnodes, NB_SITE_P2P);
                 const NodeRec sn = A.nodes[my_s];
-                my_beg = sn.begin;
-                my_cnt = sn.count;
+                my_beg = NB_IDX(sn.begin, A.n, NB_SITE_P2P);
+                my_cnt = NB_IDX(sn.count, A.n + 1 - my_beg, NB_SITE_P2P);
                 disp_s<S>(sn, nt, unit, my_dx, my_dy, my_dz);
             }
             // partners of this batch in descending particle count: the NG groups of a round then
@@ -1066,6 +1067,8 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     P2PArgs B;
     B.leaves = DP<uint32_t>(c->leaves);
     B.nleaves = c->nleaves;
+    B.nnodes = nn;
+    B.n = n;
     B.nodes = DP<NodeRec>(c->nodes);
     B.box = box;
     B.src = c->src.p;

@@ -8,3 +8,5 @@ int nb_fmm_forces_mixed(nbody_ctx* c, int integ, bool want_pot) {
 }
 
 int nb_fmm_vjp_mixed(nbody_ctx* c, double coef) { return nbfmm::vjp_dispatch<NBODY_PREC_MIXED>(c, coef); }
+
+NB_DBG_ACCESSOR(fmm_mixed)

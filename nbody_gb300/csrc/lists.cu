@@ -121,7 +121,7 @@ __device__ void lv_classify(const LevelArgs& A, uint32_t i, uint32_t* cand) {
     const uint4 it = A.item[i];
     const uint32_t t = it.x;
     uint32_t s = NONE, ns = 0, cb = 0;
-    if ((uint32_t)lane < it.z) s = A.pin_list[it.y + lane];
+    if ((uint32_t)lane < it.z) s = NB_IDX(A.pin_list[it.y + lane], A.nn, NB_SITE_LISTS);
     const NodeRec nt = A.nodes[t];
     if (s != NONE) {
         const NodeRec sn = A.nodes[s];
@@ -148,7 +148,7 @@ __device__ void lv_classify(const LevelArgs& A, uint32_t i, uint32_t* cand) {
             sc[u] = g < total ? cand[g] : NONE;
             sn[u].nchild = 0;
             sn[u].count = 0;
-            if (sc[u] != NONE) sn[u] = A.nodes[sc[u]];
+            if (sc[u] != NONE) sn[u] = A.nodes[NB_IDX(sc[u], A.nn, NB_SITE_LISTS)];
         }
 #pragma unroll
         for (int u = 0; u < CLS_UNROLL; ++u) {
@@ -310,7 +310,7 @@ __device__ __forceinline__ int moved_target(const uint32_t* cpo, int nn, uint32_
 
 __device__ __forceinline__ void move_entries(const CompactArgs& A, uint32_t d0, uint32_t tot, const uint32_t* cpo,
                                              const uint32_t* soff, const uint32_t* scnt, uint32_t* list, uint32_t base,
-                                             uint32_t* off) {
+                                             uint32_t* off, uint32_t cap) {
     const int lane = lane_id();
     int t0 = 0;
     if (lane == 0) t0 = moved_target(cpo, A.nn, d0);
@@ -325,7 +325,7 @@ __device__ __forceinline__ void move_entries(const CompactArgs& A, uint32_t d0, 
         const size_t row = (size_t)l * A.nn + t;
         const uint32_t cn = scnt[row];
         if (k < cn) {
-            list[base + d] = list[soff[row] + k];
+            list[base + d] = list[NB_IDX(soff[row] + k, cap, NB_SITE_MOVE)];
             return;
         }
         k -= cn;
@@ -346,8 +346,11 @@ __global__ void __launch_bounds__(256) k_lv_move(CompactArgs A) {
     const uint32_t cm = (tot_m + 31) / 32, cp = (tot_p + 31) / 32;
     const uint32_t stride = gridDim.x * (blockDim.x >> 5);
     for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < cm + cp; w += stride) {
-        if (w < cm) move_entries(A, 32 * w, tot_m, A.m2l_cpo, A.m2l_soff, A.m2l_scnt, A.m2l_list, em, A.m2l_off);
-        else move_entries(A, 32 * (w - cm), tot_p, A.p2p_cpo, A.p2p_soff, A.p2p_scnt, A.p2p_list, ep, A.p2p_off);
+        if (w < cm)
+            move_entries(A, 32 * w, tot_m, A.m2l_cpo, A.m2l_soff, A.m2l_scnt, A.m2l_list, em, A.m2l_off, A.m2l_cap);
+        else
+            move_entries(A, 32 * (w - cm), tot_p, A.p2p_cpo, A.p2p_soff, A.p2p_scnt, A.p2p_list, ep, A.p2p_off,
+                         A.p2p_cap);
     }
 }
 
@@ -581,3 +584,5 @@ int nb_build_lists(nbody_ctx* c) {
     }
     return nb_fail(c, NBODY_ERR_CAPACITY, "interaction lists kept overflowing");
 }
+
+NB_DBG_ACCESSOR(lists)

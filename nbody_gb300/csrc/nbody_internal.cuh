@@ -279,6 +279,47 @@ int nb_fmm_vjp_fp64(nbody_ctx* c, double coef);
 enum { NB_INTEG_NONE = 0, NB_INTEG_KDK_CLOSE = 1, NB_INTEG_EULER = 2, NB_INTEG_FAR_ONLY = 3 };
 
 // ---------------------------------------------------------------------------
+// index checks of the NBODY_DEBUG_BOUNDS build
+//
+// NB_IDX(i, n, site) is i when i < n.  In the debug build an index out of range sets bit `site` of
+// this translation unit's debug word and yields 0, an index that is always in bounds, so the kernel
+// goes on without a fault; the host reads and clears the words after each evaluation
+// (nb_dbg_check) and reports NBODY_ERR_CUDA naming the sites.  The release build compiles to i.
+// ---------------------------------------------------------------------------
+enum {
+    NB_SITE_GATHER = 0,            // sorted-order permutation entry (k_gather)
+    NB_SITE_TREE = 1,              // first particle of a node (k_tree_nodes)
+    NB_SITE_SORT = 2,              // radix scatter destination
+    NB_SITE_LISTS = 3,             // pending partner / candidate node ids (k_lv_classify)
+    NB_SITE_MOVE = 4,              // staged list entry moved behind the staged ones (k_lv_move)
+    NB_SITE_M2L = 5,               // far-field list entry (k_m2l)
+    NB_SITE_P2P = 6,               // near-field list entry and its particle range (k_p2p)
+    NB_SITE_ADJ = 7                // near-field list entry and its particle range (k_adj_p2p)
+};
+#ifdef NBODY_DEBUG_BOUNDS
+static __device__ unsigned int nb_dbg_word;     // one per translation unit
+__device__ __forceinline__ uint32_t nb_idx_check(uint64_t i, uint64_t n, int site) {
+    if (i < n) return (uint32_t)i;
+    atomicOr(&nb_dbg_word, 1u << site);
+    return 0u;
+}
+#define NB_IDX(i, n, site) nb_idx_check((uint64_t)(i), (uint64_t)(n), (site))
+// host accessor of this translation unit's word: returns it and clears it
+#define NB_DBG_ACCESSOR(name)                                                              \
+    unsigned int nb_dbg_take_##name() {                                                    \
+        unsigned int v = 0, z = 0;                                                         \
+        if (cudaMemcpyFromSymbol(&v, nb_dbg_word, sizeof(v)) != cudaSuccess) v = 0x80000000u; \
+        cudaMemcpyToSymbol(nb_dbg_word, &z, sizeof(z));                                   \
+        return v;                                                                          \
+    }
+#else
+#define NB_IDX(i, n, site) (i)
+#define NB_DBG_ACCESSOR(name)
+#endif
+// reads and clears every translation unit's debug word; NBODY_ERR_CUDA if a check fired (api.cu)
+int nb_dbg_check(nbody_ctx* c);
+
+// ---------------------------------------------------------------------------
 // device helpers
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float nb_fma(float a, float b, float c) { return fmaf(a, b, c); }

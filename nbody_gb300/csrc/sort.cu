@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_scatter(const uint64_t*
         }
         __syncthreads();
         if (valid) {
-            uint32_t pos = s_base[digit] + s_w[warp][digit] + rank;
+            uint32_t pos = NB_IDX(s_base[digit] + s_w[warp][digit] + rank, n, NB_SITE_SORT);
             kout[pos] = key;
             vout[pos] = vin[i];
         }
@@ -325,3 +325,5 @@ int nb_scan_wait_selftest(nbody_ctx* c) {
     if (c->h_info[INFO_SCAN_ERR]) return nb_fail(c, NBODY_ERR_CUDA, "a device scan did not complete in time");
     return NBODY_OK;
 }
+
+NB_DBG_ACCESSOR(sort)

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(TB) k_gather(int64_t n, const uint32_t* __rest
                                                 StatePtrs<R> b) {
     int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x;
     if (i >= n) return;
-    uint32_t j = perm[i];
+    uint32_t j = NB_IDX(perm[i], n, NB_SITE_GATHER);
     b.x[i] = a.x[j]; b.y[i] = a.y[j]; b.z[i] = a.z[j];
     b.vx[i] = a.vx[j]; b.vy[i] = a.vy[j]; b.vz[i] = a.vz[j];
     b.ax[i] = a.ax[j]; b.ay[i] = a.ay[j]; b.az[i] = a.az[j];
@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(TB) k_tree_nodes(int64_t nnodes, int64_t n, in
     int64_t k = (int64_t)blockIdx.x * TB + threadIdx.x;
     if (k >= nnodes) return;
     int l = (int)sk[k];
-    uint32_t b = sv[k];
+    uint32_t b = NB_IDX(sv[k], n, NB_SITE_TREE);
     NodeRec nd;
     nd.level = (uint8_t)l;
     nd.begin = b;
@@ -489,3 +489,5 @@ int nb_build_tree(nbody_ctx* c) {
     c->launches += 1;
     return NBODY_OK;
 }
+
+NB_DBG_ACCESSOR(tree)
