@@ -394,12 +394,17 @@ struct M2LSmem {
     typedef typename Prec<MODE>::S S;
     static constexpr int T = nb_terms<P>::value;
     static constexpr int TM = nb_tm<P>::value;
-    // 16-byte chunks per shared row must be odd: the 8 lanes of a quarter warp then read 8 distinct bank groups
-    static constexpr int SST = sizeof(S) == 4 ? ((TM / 4) % 2 ? TM : TM + 4) : TM + 2;
-    static constexpr int warps = Prec<MODE>::lane_smem ? 1 : 4;
+    // Up to order 5 in FP32 the kernel fits 128 registers, and five 3-warp blocks (15 warps) fit an
+    // SM's shared memory only with unpadded rows (2-way bank conflicts on the 16-byte row reads, a
+    // few cycles per 462 FMAs); above that, rows with an odd number of 16-byte chunks (the 8 lanes of
+    // a quarter warp then read 8 distinct bank groups) and 4-warp blocks.
+    static constexpr bool dense = sizeof(S) == 4 && P <= 5;
+    static constexpr int SST = dense ? TM : sizeof(S) == 4 ? ((TM / 4) % 2 ? TM : TM + 4) : TM + 2;
+    static constexpr int warps = Prec<MODE>::lane_smem ? 1 : dense ? 3 : 4;
+    static constexpr int min_blocks = dense ? 5 : 1;
     static constexpr size_t rows = (size_t)2 * 32 * SST * sizeof(S);
     static constexpr size_t lane_arrays = Prec<MODE>::lane_smem ? (size_t)2 * 32 * T * sizeof(S) : 0;
-    static constexpr size_t per_warp = (16 + rows + lane_arrays + 255) / 256 * 256;
+    static constexpr size_t per_warp = (16 + rows + lane_arrays + 127) / 128 * 128;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -440,7 +445,7 @@ __device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, l
 }
 
 template <int MODE, int P>
-__global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps) k_m2l(M2LArgs A) {
+__global__ void __launch_bounds__(32 * M2LSmem<MODE, P>::warps, M2LSmem<MODE, P>::min_blocks) k_m2l(M2LArgs A) {
     typedef typename Prec<MODE>::S S;
     typedef typename Prec<MODE>::H H;
     constexpr int T = nb_terms<P>::value;
