@@ -11,7 +11,7 @@ constexpr int SCAN_ITEMS = 8;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 constexpr int RADIX_THREADS = 256;
-constexpr int RADIX_ROUNDS = 16;
+constexpr int RADIX_ROUNDS = 4;           // 1,024-key tiles: enough blocks to fill the GPU at 262k keys
 constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;
 
 // exclusive block scan of one value per thread; returns the block total in *total
