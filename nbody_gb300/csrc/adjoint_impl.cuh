@@ -247,9 +247,8 @@ __device__ __forceinline__ void adj_item(const AdjP2PArgs& A, typename Prec<MODE
                 const S dx = __shfl_sync(0xffffffffu, my_dx, qs), dy = __shfl_sync(0xffffffffu, my_dy, qs),
                         dz = __shfl_sync(0xffffffffu, my_dz, qs);
                 const uint32_t scnt = q < nbat ? scnt0 : 0u;
-                uint32_t mx = scnt;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                // the round's largest partner: partners are sorted by particle count, so it is the first
+                const uint32_t mx = __shfl_sync(0xffffffffu, my_cnt, (rr * NG) & 31);
                 const bool self = s_id == k && q < nbat;
                 S xs[TPL][3];
 #pragma unroll

@@ -789,9 +789,8 @@ __device__ __forceinline__ void p2p_item(const P2PArgs& A, typename Prec<MODE>::
                         dz = __shfl_sync(0xffffffffu, my_dz, qs);
                 const uint32_t scnt0 = __shfl_sync(0xffffffffu, my_cnt, qs);
                 const uint32_t scnt = q < nb ? scnt0 : 0u;
-                uint32_t mx = scnt;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                // the round's largest partner: partners are sorted by particle count, so it is the first
+                const uint32_t mx = __shfl_sync(0xffffffffu, my_cnt, (rr * NG) & 31);
 #pragma unroll
                 for (int e = 0; e < EPL; ++e) gtile[gl + e * CT] = pre[e];
                 __syncwarp();
