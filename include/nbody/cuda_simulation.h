@@ -197,6 +197,11 @@ public:
         check(nbody_set_timestep_control(_ctx, NBODY_DT_ADAPTIVE, eta, length, dtMin, dtMax),
               "nbody_set_timestep_control");
     }
+    /* individual steps dtMax / 2^k per particle (dtMax / dtMin = 2^K), each from eta sqrt(length / |a_i|) */
+    void setBlockTimesteps(double eta, double length, double dtMin, double dtMax) {
+        check(nbody_set_timestep_control(_ctx, NBODY_DT_BLOCK, eta, length, dtMin, dtMax),
+              "nbody_set_timestep_control");
+    }
     void setFixedTimestep() {
         check(nbody_set_timestep_control(_ctx, NBODY_DT_FIXED, 0.0, 0.0, 0.0, 0.0), "nbody_set_timestep_control");
     }

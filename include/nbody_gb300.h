@@ -113,7 +113,22 @@ int nbody_step(nbody_ctx* c, int nsteps, double* t_out);
    NBODY_DT_FIXED restores the dt the context had before. */
 #define NBODY_DT_FIXED 0
 #define NBODY_DT_ADAPTIVE 1
+#define NBODY_DT_BLOCK 2
 int nbody_set_timestep_control(nbody_ctx* c, int mode, double eta, double length, double dt_min, double dt_max);
+
+/* mode NBODY_DT_BLOCK (leapfrog only): individual time steps in a power-of-two
+   hierarchy.  dt_max / dt_min must be 2^K (K <= 20).  Each nbody_step
+   advances dt_max in 2^K substeps of dt_min: every particle drifts every
+   substep; particle i takes steps of dt_i = dt_max / 2^k_i, with k_i the
+   smallest level whose step is no longer than eta sqrt(length / |a_i|)
+   (length <= 0: eps), chosen at the start of each of its steps from its
+   acceleration there (a step may only start where the substep grid allows
+   it), and receives its half kicks at the start and the end of each of its
+   steps.  Every substep evaluates all forces.  At the end of nbody_step all
+   particles are synchronous.  K = 0 is the fixed-step kick-drift-kick
+   leapfrog.  nbody_get_levels gives each particle's k (input order) of its
+   last step; nbody_last_timestep returns dt_max. */
+int nbody_get_levels(nbody_ctx* c, int32_t* levels);
 
 /* Particles that leave a fixed root box (params.fixed_box = 1).  The
    reference builds its octree over [0, bounds) (src/open_cl_simulation.cpp:

@@ -20,7 +20,7 @@ ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: 
 
 PREC_FP32, PREC_MIXED, PREC_FP64 = 0, 1, 2
 INTEG_LEAPFROG, INTEG_EULER = 0, 1
-DT_FIXED, DT_ADAPTIVE = 0, 1
+DT_FIXED, DT_ADAPTIVE, DT_BLOCK = 0, 1, 2
 ESCAPE_GROW, ESCAPE_ERROR = 0, 1
 
 EXPORTS = ("nbody_default_params", "nbody_create", "nbody_destroy", "nbody_set_state", "nbody_get_state",
@@ -30,7 +30,7 @@ EXPORTS = ("nbody_default_params", "nbody_create", "nbody_destroy", "nbody_set_s
            "nbody_measure_peaks", "nbody_direct_forces_static", "nbody_force_vjp", "nbody_forward_checkpointed",
            "nbody_backward", "nbody_device_memory", "nbody_trajectory_open", "nbody_trajectory_close",
            "nbody_set_timestep_control", "nbody_last_timestep", "nbody_set_escape_policy", "nbody_set_wait_limits",
-           "nbody_selftest_wait", "nbody_forward_replay", "nbody_debug_bounds")
+           "nbody_selftest_wait", "nbody_forward_replay", "nbody_debug_bounds", "nbody_get_levels")
 
 
 class Params(C.Structure):
@@ -101,6 +101,7 @@ def load(path: str | None = None):
     L.nbody_selftest_wait.argtypes = [vp, C.c_int]
     L.nbody_forward_replay.argtypes = [vp, vp, vp, vp, vp, C.c_int, vp, vp]
     L.nbody_debug_bounds.argtypes = []
+    L.nbody_get_levels.argtypes = [vp, vp]
     L.nbody_last_error.argtypes = [vp]
     L.nbody_last_error.restype = C.c_char_p
     for name in EXPORTS:

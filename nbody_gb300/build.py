@@ -22,7 +22,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnbody_gb300.so")
 BUILD_DEBUG = os.path.join(HERE, "_build_debug")
 LIB_DEBUG = os.path.join(HERE, "libnbody_gb300_debug.so")
-UNITS = ["api.cu", "sort.cu", "tree.cu", "direct.cu", "direct_static.cu", "fmm_fp32.cu", "fmm_mixed.cu", "fmm_fp64.cu", "adjoint.cu", "lists.cu", "trajectory.cu"]
+UNITS = ["api.cu", "sort.cu", "tree.cu", "direct.cu", "direct_static.cu", "fmm_fp32.cu", "fmm_mixed.cu", "fmm_fp64.cu", "adjoint.cu", "lists.cu", "trajectory.cu", "blocksteps.cu"]
 HEADERS = ["nbody_internal.cuh", "fmm_impl.cuh", "adjoint_impl.cuh", "fmm_ops.inc", "../../include/nbody_gb300.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",

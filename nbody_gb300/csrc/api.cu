@@ -539,6 +539,13 @@ int nbody_step(nbody_ctx* c, int nsteps, double* t_out) {
     NB_CU(c, cudaSetDevice(c->device));
     if (nsteps > 0) c->ck_steps = 0;
     for (int s = 0; s < nsteps; ++s) {
+        if (c->dt_mode == NBODY_DT_BLOCK) {
+            NB_TRY(nb_block_step(c));
+            c->dt_last = c->dt_max;
+            c->time += c->dt_max;
+            NB_TRY(nb_traj_capture(c));
+            continue;
+        }
         if (c->dt_mode == NBODY_DT_ADAPTIVE) {
             // this step's dt needs the largest acceleration at the current positions (leapfrog) or
             // of the last evaluation (Euler); without one, evaluate the forces first
@@ -695,12 +702,22 @@ int nbody_device_memory(nbody_ctx* c, int64_t* current, int64_t* peak) {
 int nbody_set_timestep_control(nbody_ctx* c, int mode, double eta, double length, double dt_min, double dt_max) {
     if (!c) return NBODY_ERR_INVALID;
     if (mode == NBODY_DT_FIXED) {
-        if (c->dt_mode == NBODY_DT_ADAPTIVE) c->prm.dt = c->dt_base;
+        if (c->dt_mode != NBODY_DT_FIXED) c->prm.dt = c->dt_base;
         c->dt_mode = NBODY_DT_FIXED;
         c->amax_valid = false;
         return NBODY_OK;
     }
-    if (mode != NBODY_DT_ADAPTIVE) return nb_fail(c, NBODY_ERR_INVALID, "mode must be NBODY_DT_FIXED or NBODY_DT_ADAPTIVE");
+    if (mode != NBODY_DT_ADAPTIVE && mode != NBODY_DT_BLOCK)
+        return nb_fail(c, NBODY_ERR_INVALID, "mode must be NBODY_DT_FIXED, NBODY_DT_ADAPTIVE or NBODY_DT_BLOCK");
+    int K = 0;
+    if (mode == NBODY_DT_BLOCK) {
+        if (c->prm.integrator != NBODY_INTEG_LEAPFROG)
+            return nb_fail(c, NBODY_ERR_INVALID, "block time steps need the leapfrog integrator");
+        const double r = dt_max / dt_min;
+        while (K < 20 && (double)(1 << K) < r * (1.0 - 1e-12)) ++K;
+        if (!(dt_min > 0.0) || !(std::fabs((double)(1 << K) - r) <= 1e-9 * r))
+            return nb_fail(c, NBODY_ERR_INVALID, "block steps need dt_max / dt_min = 2^K, K <= 20");
+    }
     if (!(eta > 0.0) || !std::isfinite(eta)) return nb_fail(c, NBODY_ERR_INVALID, "eta must be > 0");
     if (!(dt_min > 0.0) || !(dt_max >= dt_min) || !std::isfinite(dt_max))
         return nb_fail(c, NBODY_ERR_INVALID, "need 0 < dt_min <= dt_max < inf");
@@ -711,7 +728,9 @@ int nbody_set_timestep_control(nbody_ctx* c, int mode, double eta, double length
     NB_TRY(nb_grow(c, c->amax, sizeof(unsigned long long)));
     if (!c->h_amax) NB_CU(c, cudaMallocHost(&c->h_amax, sizeof(double)));
     if (c->dt_mode == NBODY_DT_FIXED) c->dt_base = c->prm.dt;
-    c->dt_mode = NBODY_DT_ADAPTIVE;
+    c->dt_mode = mode;
+    c->blk_K = K;
+    if (mode == NBODY_DT_BLOCK) c->prm.dt = dt_max;
     c->dt_eta = eta;
     c->dt_len = length;
     c->dt_min = dt_min;

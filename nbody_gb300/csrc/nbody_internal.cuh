@@ -195,6 +195,11 @@ struct nbody_ctx {
     double dt_base = 0;            // params.dt before adaptive steps were switched on
     double dt_last = 0;            // dt of the last step
     bool amax_valid = false;       // amax2 holds max |a|^2 of the current accelerations
+    int blk_K = 0;                 // block steps: substeps of dt_max / 2^blk_K (NBODY_DT_BLOCK)
+    double blk_dt = 0;             // the substep (drift) length
+    DevBuf blk_level;              // per input id: level k of the particle's current step, dt = dt_max / 2^k
+    DevBuf blk_count;              // per level: closing kicks of the last base step
+    unsigned int h_blk_count[32] = {0};
     double amax2 = 0;
     DevBuf amax;                   // device word of the reduction (bits of a non-negative double)
     double* h_amax = nullptr;      // pinned copy
@@ -264,6 +269,8 @@ int nb_traj_close(nbody_ctx* c);
 int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot);
 // the far and near field only, on the tree and lists already loaded (lists_frozen) (api.cu)
 int nb_evaluate_frozen(nbody_ctx* c, int integ);
+// one base step of dt_max with block (individual power-of-two) time steps (blocksteps.cu)
+int nb_block_step(nbody_ctx* c);
 
 // fmm (fmm_*.cu)
 int nb_fmm_forces_fp32(nbody_ctx* c, int integ, bool want_pot);

@@ -57,10 +57,13 @@ __global__ void __launch_bounds__(TB) k_kick_drift_bbox(int64_t n, StatePtrs<R> 
     bool bad = false;
     for (int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x; i < n; i += (int64_t)gridDim.x * TB) {
         R x = s.x[i], y = s.y[i], z = s.z[i];
-        if (kdk) {
+        if (kdk == 1) {
             R vx = s.vx[i] + (R)hdt * s.ax[i], vy = s.vy[i] + (R)hdt * s.ay[i], vz = s.vz[i] + (R)hdt * s.az[i];
             x += (R)dt * vx; y += (R)dt * vy; z += (R)dt * vz;
             s.vx[i] = vx; s.vy[i] = vy; s.vz[i] = vz;
+            s.x[i] = x; s.y[i] = y; s.z[i] = z;
+        } else if (kdk == 2) {             // drift only (block steps: the kicks are per particle)
+            x += (R)dt * s.vx[i]; y += (R)dt * s.vy[i]; z += (R)dt * s.vz[i];
             s.x[i] = x; s.y[i] = y; s.z[i] = z;
         }
         const double p[3] = {(double)x, (double)y, (double)z};
@@ -369,7 +372,8 @@ int begin_step_t(nbody_ctx* c, int kdk) {
     unsigned g = nblk(n);
     if (g > 152 * 8) g = 152 * 8;
     if (g == 0) g = 1;
-    k_kick_drift_bbox<R><<<g, TB, 0, c->st>>>(n, state<R>(c, c->cur), 0.5 * c->prm.dt, c->prm.dt, kdk, bb,
+    const double dt = kdk == 2 ? c->blk_dt : c->prm.dt;
+    k_kick_drift_bbox<R><<<g, TB, 0, c->st>>>(n, state<R>(c, c->cur), 0.5 * dt, dt, kdk, bb,
                                               DP<int32_t>(c->info));
     k_box<<<1, 1, 0, c->st>>>(bb, c->prm.fixed_box, c->escape_policy == NBODY_ESCAPE_GROW, c->prm.box_min[0],
                               c->prm.box_min[1], c->prm.box_min[2], c->prm.box_size, DP<BoxDev>(c->box),

@@ -254,10 +254,18 @@ class CudaSimulation:
     def set_timestep_control(self, mode: str = "adaptive", eta: float = 0.02, length: float = 0.0,
                              dt_min: float = 1e-8, dt_max: float = 1e-2):
         """Adaptive global step: dt = clamp(eta * sqrt(length / max|a|), dt_min, dt_max) from the last
-        evaluation's accelerations (length <= 0: the softening eps); mode "fixed" restores params.dt."""
-        m = {"fixed": _lib.DT_FIXED, "adaptive": _lib.DT_ADAPTIVE}[mode]
+        evaluation's accelerations (length <= 0: the softening eps); mode "block": individual steps
+        dt_max / 2^k per particle from the same criterion on its own |a|, dt_max / dt_min = 2^K substeps
+        per step(); mode "fixed" restores params.dt."""
+        m = {"fixed": _lib.DT_FIXED, "adaptive": _lib.DT_ADAPTIVE, "block": _lib.DT_BLOCK}[mode]
         check(self._h, _lib.load().nbody_set_timestep_control(self._h, m, float(eta), float(length), float(dt_min),
                                                               float(dt_max)))
+
+    def levels(self):
+        """Block steps: each particle's level k (input order) of its last step, dt = dt_max / 2^k."""
+        out = np.empty(self.n, np.int32)
+        check(self._h, _lib.load().nbody_get_levels(self._h, ptr(out)))
+        return out
 
     def last_timestep(self) -> float:
         """dt of the last step taken."""

@@ -335,6 +335,50 @@ def leapfrog_adaptive(pos, vel, q, m, eps, G, eta, length, dt_min, dt_max, steps
     return pos, vel, acc, np.array(dts)
 
 
+def block_level(acc, eta, length, dt_max, K):
+    """Level k of each particle for block steps: the smallest k in 0..K with dt_max 2^-k <=
+    eta sqrt(length / |a|), |a|^2 summed as x*x + y*y + z*z (the library's rule; the reference only
+    lists a variable time step as a goal)."""
+    acc = np.asarray(acc, dtype=np.float64).reshape(-1, 3)
+    a2 = acc[:, 0] * acc[:, 0] + acc[:, 1] * acc[:, 1] + acc[:, 2] * acc[:, 2]
+    k = np.zeros(len(a2), np.int64)
+    pos = a2 > 0
+    want = np.full(len(a2), np.inf)
+    want[pos] = eta * np.sqrt(length / np.sqrt(a2[pos]))
+    for _ in range(K):
+        step = np.ldexp(dt_max, -k)
+        k = np.where((k < K) & (step > want), k + 1, k)
+    return k
+
+
+def leapfrog_block(pos, vel, q, m, eps, G, eta, length, dt_max, K, steps, nthreads=None):
+    """FP64 direct-sum kick-drift-kick leapfrog with individual power-of-two steps (the library's
+    NBODY_DT_BLOCK scheme): per base step dt_max, 2^K substeps of dt_max 2^-K; every particle drifts
+    every substep; a particle's step of dt_max 2^-k starts with a half kick and ends with one, and
+    its level comes from block_level at the start of each of its steps, no coarser than the substep
+    grid allows there.  Returns (pos, vel, acc, levels of the last steps)."""
+    x = np.array(pos, dtype=np.float64).reshape(-1, 3)
+    v = np.array(vel, dtype=np.float64).reshape(-1, 3)
+    length = length if length > 0.0 else eps
+    a = direct(x, q, m, eps, G, nthreads=nthreads)[0]
+    S = 1 << K
+    lv = None
+    for _ in range(steps):
+        lv = block_level(a, eta, length, dt_max, K)
+        v = v + np.ldexp(dt_max, -(lv + 1))[:, None] * a
+        for s in range(1, S + 1):
+            x = x + np.ldexp(dt_max, -K) * v
+            a = direct(x, q, m, eps, G, nthreads=nthreads)[0]
+            end = (s & ((1 << (K - lv)) - 1)) == 0
+            v = v + np.where(end, np.ldexp(dt_max, -(lv + 1)), 0.0)[:, None] * a
+            if s < S:
+                tz = (s & -s).bit_length() - 1
+                new = np.maximum(block_level(a, eta, length, dt_max, K), K - tz)
+                lv = np.where(end, new, lv)
+                v = v + np.where(end, np.ldexp(dt_max, -(lv + 1)), 0.0)[:, None] * a
+    return x, v, a, lv
+
+
 def direct_vjp(pos, q, m, mu, eps=0.01, G=1.0, nthreads=None):
     """FP64 direct-sum VJP of S = sum_i mu_i . a_i: (dS/dx, dS/dq, dS/dm)."""
     pos = np.ascontiguousarray(pos, np.float64).reshape(-1)

@@ -80,3 +80,48 @@ def test_adaptive_clamps_modes_and_refusals(nb):
     p, _, _, _, _ = sim.state("input")
     assert np.all(np.isfinite(p))
     sim.close()
+
+
+def test_block_steps_match_fp64_direct(nb, oracle):
+    """Individual power-of-two steps (NBODY_DT_BLOCK, K = 3: dt_max 8e-3, substeps of 1e-3) against the
+    oracle's FP64 direct-sum restatement: the same level for every particle (the FP64 order-8 forces
+    are within ~1e-8 of the direct sum, far from a level threshold), positions within 1e-7 and
+    velocities within 1e-5, as for the adaptive global step; several levels in use."""
+    pos, vel, m = ics.plummer(1024, seed=64)
+    eta, dt_min, dt_max, steps = 0.02, 1e-3, 8e-3, 2
+    sim = _sim(nb, pos, vel, m)
+    sim.set_timestep_control("block", eta=eta, length=0.0, dt_min=dt_min, dt_max=dt_max)
+    sim.step(steps)
+    assert sim.last_timestep() == dt_max
+    assert sim.time == pytest.approx(steps * dt_max, rel=1e-14, abs=0)
+    lv = sim.levels()
+    p1, v1, _, _, _ = sim.state("input")
+    p2, v2, _, lv2 = oracle.leapfrog_block(pos, vel, m, m, 0.01, 1.0, eta, 0.0, dt_max, 3, steps)
+    np.testing.assert_array_equal(lv, lv2)
+    assert len(np.unique(lv)) >= 2, np.bincount(lv)
+    assert np.abs(p1 - p2).max() < 1e-7
+    assert np.abs(v1 - v2).max() < 1e-5
+    # the recorded run of the adjoint refuses block steps; back to the fixed step
+    with pytest.raises(nb.NbodyError):
+        sim.forward_checkpointed(2, 0)
+    sim.set_timestep_control("fixed")
+    sim.step()
+    assert sim.last_timestep() == 1e-3
+    sim.close()
+
+
+def test_block_steps_with_one_level_are_the_fixed_leapfrog(nb):
+    """K = 0 (dt_min = dt_max): the block scheme is the fixed-step kick-drift-kick leapfrog, computed by
+    separate kick and drift kernels instead of the fused ones: equal to 1e-14."""
+    pos, vel, m = ics.plummer(2048, seed=65)
+    a = _sim(nb, pos, vel, m, precision=nb.PREC_MIXED, order=5, leaf_capacity=16, dt=2e-3)
+    a.step(3)
+    b = _sim(nb, pos, vel, m, precision=nb.PREC_MIXED, order=5, leaf_capacity=16, dt=2e-3)
+    b.set_timestep_control("block", eta=0.02, length=0.0, dt_min=2e-3, dt_max=2e-3)
+    b.step(3)
+    pa, va = a.state("input")[:2]
+    pb, vb = b.state("input")[:2]
+    np.testing.assert_allclose(pb, pa, rtol=0, atol=1e-14)
+    np.testing.assert_allclose(vb, va, rtol=0, atol=1e-13)
+    with pytest.raises(nb.NbodyError):
+        b.set_timestep_control("block", eta=0.02, length=0.0, dt_min=3e-4, dt_max=2e-3)   # not 2^K

@@ -342,3 +342,22 @@ def test_grown_box_rule(oracle):
         assert np.all(a == np.round(a)) and np.all(a >= 0) and np.all(a < k)
         if k > 1:
             assert not (np.all(a < k / 2) and np.all(o + s / 2 > p.max(axis=0)))
+
+
+def test_block_leapfrog_reduces_to_the_fixed_step(oracle):
+    """oracle.leapfrog_block with K = 0 is the kick-drift-kick leapfrog of oracle.leapfrog; with K > 0
+    its levels follow block_level and every level is used on a Plummer core."""
+    import numpy as np
+    from nbody_gb300 import ics
+    pos, vel, m = ics.plummer(512, seed=9)
+    x0, v0, a0 = oracle.leapfrog(pos, vel, m, m, 0.01, 1.0, 2e-3, 3)
+    x1, v1, a1, lv = oracle.leapfrog_block(pos, vel, m, m, 0.01, 1.0, 0.05, 0.0, 2e-3, 0, 3)
+    np.testing.assert_allclose(x1, x0, rtol=0, atol=1e-14)
+    np.testing.assert_allclose(v1, v0, rtol=0, atol=1e-13)
+    assert np.all(lv == 0)
+    x2, v2, a2, lv2 = oracle.leapfrog_block(pos, vel, m, m, 0.01, 1.0, 0.02, 0.0, 8e-3, 3, 2)
+    assert np.all((lv2 >= 0) & (lv2 <= 3)) and len(np.unique(lv2)) >= 2
+    # a finer global step moves toward the block result more than the coarse one does
+    xf, _, _ = oracle.leapfrog(pos, vel, m, m, 0.01, 1.0, 1e-3, 16)
+    xc, _, _ = oracle.leapfrog(pos, vel, m, m, 0.01, 1.0, 8e-3, 2)
+    assert np.abs(x2 - xf).max() < np.abs(xc - xf).max()
