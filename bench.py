@@ -196,6 +196,9 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of each FP64 configuration")
     ap.add_argument("--drift-steps", type=int, default=1000,
                     help="leapfrog steps of the energy / momentum drift run from the initial state (0: skip)")
+    ap.add_argument("--block-K", type=int, default=0,
+                    help="also time individual block steps with dt_max = dt * 2^K (0: skip)")
+    ap.add_argument("--block-eta", type=float, default=0.02)
     a = ap.parse_args()
     assert a.warmup >= 0 and a.steps >= 1
     rank, world, local = dist_env()
@@ -407,6 +410,35 @@ def main():
                          "timed run); total mass 1"}
         sd.close()
 
+    # individual block steps: dt_min = dt, dt_max = dt 2^K, on the same initial state; compared with the
+    # fixed step dt over the same simulated time
+    block = None
+    if a.block_K > 0:
+        sb = nb.CudaSimulation.from_arrays(pos, vel, m, m, precision=prec, order=a.order, leaf_capacity=a.cap,
+                                           theta=a.theta, eps=a.eps, dt=a.dt, integrator=nb.INTEG_LEAPFROG,
+                                           fixed_box=0, device=local)
+        sb.set_timestep_control("block", eta=a.block_eta, length=0.0, dt_min=a.dt, dt_max=a.dt * (1 << a.block_K))
+        sb.step(1)
+        stb = torch.cuda.ExternalStream(sb.stream, device=torch.device("cuda", local))
+        torch.cuda.synchronize()
+        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b0.record(stb)
+        nbs = 2
+        sb.step(nbs)
+        b1.record(stb)
+        torch.cuda.synchronize()
+        ms_b = b0.elapsed_time(b1) / nbs
+        st = sb.stats()
+        block = {"K": a.block_K, "eta": a.block_eta, "dt_min": a.dt, "dt_max": a.dt * (1 << a.block_K),
+                 "ms_per_base_step": ms_b, "fixed_ms_same_time": ms / a.steps * (1 << a.block_K),
+                 "speedup_vs_fixed_dt_min": ms / a.steps * (1 << a.block_K) / ms_b,
+                 "levels": np.bincount(sb.levels(), minlength=a.block_K + 1).tolist(),
+                 "near_field_leaves_evaluated_frac": st["block_active_leaves"] / max(st["block_leaves"], 1),
+                 "note": "time per base step of dt_max (2^K substeps, every particle drifted, forces evaluated "
+                         "on the whole tree, near field only for leaves with a particle closing its step) vs "
+                         "2^K fixed steps of dt_min"}
+        sb.close()
+
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -451,7 +483,7 @@ def main():
         "data": f"synthetic seeded collision ICs (seed {a.seed} + rank)", "config": workload_desc(a),
         "rms_force_err_vs_fp64_direct": rms_err, "max_force_err_vs_fp64_direct": max_err,
         "err_targets": int(len(tg)), "fwd_adjoint": fwd_adj, "fp64_equal_error": fp64_cmp,
-        "energy_momentum_drift": drift,
+        "energy_momentum_drift": drift, "block_steps": block,
         "phase_ms_per_step": {k: float(v) for k, v in zip(nb.CudaSimulation.PHASES, per_step)},
         "work_per_step": stats, "wall_s_timed": wall,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": a.n * 8 * 11, "d2h_bytes_per_step": a.n * 8 * 9,

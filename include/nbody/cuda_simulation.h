@@ -216,8 +216,8 @@ public:
        step() throw; grownBoxes() counts the evaluations that took a grown box */
     void setEscapePolicy(int policy) { check(nbody_set_escape_policy(_ctx, policy), "nbody_set_escape_policy"); }
     int64_t grownBoxes() const {
-        int64_t s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        check(nbody_get_stats(_ctx, s, 8), "nbody_get_stats");
+        int64_t s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        check(nbody_get_stats(_ctx, s, 10), "nbody_get_stats");
         return s[7];
     }
 

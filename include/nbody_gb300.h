@@ -261,8 +261,10 @@ int nbody_direct_forces_static(int device, int64_t n, const double* pos, const d
    cell pairs, out[1] near-field particle pairs, out[2] near-field leaf
    pairs, out[3] nodes, out[4] leaves, out[5] depth, out[6] kernel launches
    of the last step, out[7] evaluations since nbody_set_state whose fixed
-   root box was grown (nbody_set_escape_policy).  n = number of entries
-   wanted (<= 8). */
+   root box was grown (nbody_set_escape_policy), out[8] near-field leaves
+   over the substeps of the last block step and out[9] how many of them
+   held a particle closing its step (the others' near field was skipped).
+   n = number of entries wanted (<= 10). */
 int nbody_get_stats(nbody_ctx* c, int64_t* out, int n);
 
 /* Floating-point operations this build counts per far-field cell pair

@@ -62,6 +62,24 @@ __global__ void __launch_bounds__(TB) k_block_kick(int64_t n, R* __restrict__ vx
     vx[i] = v0; vy[i] = v1; vz[i] = v2;
 }
 
+// per leaf (near-field order): does one of its particles close its step at substep s?
+__global__ void __launch_bounds__(TB) k_block_active(int64_t nleaves, const uint32_t* __restrict__ leaves,
+                                                      const NodeRec* __restrict__ nodes,
+                                                      const uint32_t* __restrict__ id,
+                                                      const uint8_t* __restrict__ level, int K, int s,
+                                                      uint8_t* __restrict__ active, unsigned int* __restrict__ count) {
+    const int64_t li = (int64_t)blockIdx.x * TB + threadIdx.x;
+    if (li >= nleaves) return;
+    const NodeRec nd = nodes[leaves[li]];
+    uint8_t a = 0;
+    for (uint32_t i = nd.begin; i < nd.begin + nd.count && !a; ++i) {
+        const int k = level[id[i]];
+        a = (s & ((1 << (K - k)) - 1)) == 0;
+    }
+    active[li] = a;
+    if (a) atomicAdd(count, 1u);
+}
+
 template <typename R>
 int block_kick(nbody_ctx* c, int s) {
     const int k = c->cur;
@@ -76,6 +94,18 @@ int block_kick(nbody_ctx* c, int s) {
 
 }  // namespace
 
+int nb_block_active_leaves(nbody_ctx* c) {
+    NB_TRY(nb_grow(c, c->blk_active, (size_t)c->nleaves + 1));
+    k_block_active<<<nblk(c->nleaves), TB, 0, c->st>>>(c->nleaves, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes),
+                                                       DP<uint32_t>(c->id[c->cur]), DP<uint8_t>(c->blk_level),
+                                                       c->blk_K, c->blk_s, DP<uint8_t>(c->blk_active),
+                                                       DP<unsigned int>(c->blk_count) + 31);
+    NB_LAUNCHED(c, "block active leaves");
+    c->launches += 1;
+    c->blk_leaves += c->nleaves;
+    return NBODY_OK;
+}
+
 int nb_block_step(nbody_ctx* c) {
     NB_TRY(nb_grow(c, c->blk_level, (size_t)c->n));
     NB_TRY(nb_grow(c, c->blk_count, sizeof(unsigned int) * 32));
@@ -87,12 +117,19 @@ int nb_block_step(nbody_ctx* c) {
     c->blk_dt = ldexp(c->dt_max, -c->blk_K);
     NB_TRY(c->rsz == 4 ? block_kick<float>(c, 0) : block_kick<double>(c, 0));
     const int S = 1 << c->blk_K;
+    c->blk_leaves = 0;
     for (int s = 1; s <= S; ++s) {
-        NB_TRY(nb_evaluate(c, 2, NB_INTEG_NONE, false));      // drift of every particle + forces
+        // drift of every particle + forces; near field and L2P only for leaves holding a particle whose
+        // step ends at s (the others' accelerations are not used at this substep)
+        c->blk_s = s;
+        const int rc = nb_evaluate(c, 2, NB_INTEG_NONE, false);
+        c->blk_s = 0;
+        NB_TRY(rc);
         NB_TRY(c->rsz == 4 ? block_kick<float>(c, s) : block_kick<double>(c, s));
     }
     NB_CU(c, cudaMemcpyAsync(c->h_blk_count, c->blk_count.p, sizeof(unsigned int) * 32, cudaMemcpyDeviceToHost, c->st));
     NB_CU(c, cudaStreamSynchronize(c->st));
+    c->blk_active_leaves = c->h_blk_count[31];
     return NBODY_OK;
 }
 

@@ -637,6 +637,8 @@ struct P2PArgs {
     void* pot;              // R* or null
     double eps2, G, dt;
     int integ;
+    const uint8_t* leaf_active;   // block steps: per leaf (near-field order), 0 = no particle closes a step
+                                  // at this substep, its near field and L2P are skipped; null: every leaf
 };
 
 template <typename S>
@@ -883,6 +885,7 @@ __global__ void __launch_bounds__(32 * P2P_WARPS, P2PShape<CLS>::TPL == 3 ? 4 : 
     const uint32_t w = w_lo + blockIdx.x * P2P_WARPS + wib;
     if (w >= w_hi) return;
     const int64_t li = p2p_leaf_of(A.work_off, li_lo, li_hi, w);
+    if (A.leaf_active && !A.leaf_active[li]) return;
     const uint32_t chunk = w - A.work_off[li];
     const uint32_t nchunk = A.work_off[li + 1] - A.work_off[li];
     const uint32_t k = A.leaves[li];
@@ -914,6 +917,7 @@ __global__ void __launch_bounds__(32 * P2P_WARPS) k_p2p_final(P2PArgs A) {
     if (li >= A.nleaves) return;
     const uint32_t nchunk = A.work_off[li + 1] - A.work_off[li];
     if (nchunk <= 1) return;
+    if (A.leaf_active && !A.leaf_active[li]) return;
     const uint32_t k = A.leaves[li];
     const NodeRec nt = A.nodes[k];
     const H* Lg = (const H*)A.L;
@@ -1091,6 +1095,11 @@ int fmm_forces(nbody_ctx* c, int integ, bool want_pot) {
     B.G = c->prm.G;
     B.dt = c->prm.dt;
     B.integ = integ;
+    B.leaf_active = nullptr;
+    if (c->blk_s > 0) {
+        NB_TRY(nb_block_active_leaves(c));
+        B.leaf_active = DP<uint8_t>(c->blk_active);
+    }
     const unsigned gf = (unsigned)((nl + P2P_WARPS - 1) / P2P_WARPS);
     {
         const int rc = want_pot ? p2p_launch_classes<MODE, P, true>(c, B) : p2p_launch_classes<MODE, P, false>(c, B);

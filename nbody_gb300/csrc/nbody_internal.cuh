@@ -199,6 +199,9 @@ struct nbody_ctx {
     double blk_dt = 0;             // the substep (drift) length
     DevBuf blk_level;              // per input id: level k of the particle's current step, dt = dt_max / 2^k
     DevBuf blk_count;              // per level: closing kicks of the last base step
+    DevBuf blk_active;             // per leaf (near-field order): a particle closes its step at substep blk_s
+    int blk_s = 0;                 // substep of the evaluation in progress (0: not a block substep)
+    int64_t blk_leaves = 0, blk_active_leaves = 0;   // near-field leaves evaluated vs skipped (stats)
     unsigned int h_blk_count[32] = {0};
     double amax2 = 0;
     DevBuf amax;                   // device word of the reduction (bits of a non-negative double)
@@ -271,6 +274,8 @@ int nb_evaluate(nbody_ctx* c, int kdk, int integ, bool want_pot);
 int nb_evaluate_frozen(nbody_ctx* c, int integ);
 // one base step of dt_max with block (individual power-of-two) time steps (blocksteps.cu)
 int nb_block_step(nbody_ctx* c);
+// marks the near-field leaves holding a particle whose step ends at substep blk_s (blocksteps.cu)
+int nb_block_active_leaves(nbody_ctx* c);
 
 // fmm (fmm_*.cu)
 int nb_fmm_forces_fp32(nbody_ctx* c, int integ, bool want_pot);

@@ -280,10 +280,10 @@ class CudaSimulation:
         return cur.value, peak.value
 
     def stats(self):
-        out = np.zeros(8, np.int64)
-        check(self._h, _lib.load().nbody_get_stats(self._h, ptr(out), 8))
+        out = np.zeros(10, np.int64)
+        check(self._h, _lib.load().nbody_get_stats(self._h, ptr(out), 10))
         keys = ("m2l_pairs", "p2p_particle_pairs", "p2p_leaf_pairs", "nodes", "leaves", "depth", "launches",
-                "grown_boxes")
+                "grown_boxes", "block_leaves", "block_active_leaves")
         return dict(zip(keys, (int(v) for v in out)))
 
     def set_escape_policy(self, policy: str = "grow"):

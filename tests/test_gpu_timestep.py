@@ -99,6 +99,8 @@ def test_block_steps_match_fp64_direct(nb, oracle):
     p2, v2, _, lv2 = oracle.leapfrog_block(pos, vel, m, m, 0.01, 1.0, eta, 0.0, dt_max, 3, steps)
     np.testing.assert_array_equal(lv, lv2)
     assert len(np.unique(lv)) >= 2, np.bincount(lv)
+    st = sim.stats()                      # some substeps skipped the near field of some leaves
+    assert 0 < st["block_active_leaves"] < st["block_leaves"], st
     assert np.abs(p1 - p2).max() < 1e-7
     assert np.abs(v1 - v2).max() < 1e-5
     # the recorded run of the adjoint refuses block steps; back to the fixed step
