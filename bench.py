@@ -453,22 +453,26 @@ def main():
     m2l_flops = stats["m2l_pairs"] * L.nbody_flops_per_m2l(a.order)
     p2p_tf = p2p_flops / (per_step[6] * 1e-3) / 1e12 if per_step[6] > 0 else 0.0
     m2l_tf = m2l_flops / (per_step[5] * 1e-3) / 1e12 if per_step[5] > 0 else 0.0
-    # DRAM bytes per step of each kernel group (dram__bytes_read.sum + dram__bytes_write.sum), from an
-    # ncu launch list of this default workload; other configurations have no capture
-    default_cfg = (a.n, a.order, a.cap, a.precision, a.theta) == (1048576, 5, 64, "mixed", 0.5)
+    # DRAM bytes per step of each kernel group (dram__bytes_read.sum + dram__bytes_write.sum), from
+    # one-kernel ncu captures of the same collision at N = 262,144, scaled to this N: the near field's
+    # 59.0 MB by the particle count (its DRAM traffic is per particle: sources are re-read from L2),
+    # M2L's 49.2 MB (11.2 M cell pairs) by the cell pairs (its list entries); other configurations have
+    # no capture
+    default_cfg = (a.order, a.cap, a.precision, a.theta) == (5, 64, "mixed", 0.5)
     kernels = {
         "k_p2p": {"ms": per_step[6], "tflops": p2p_tf, "flops_per_launch": p2p_flops, "launches": 7,
                   "phase": "near field + L2P + integrator: six leaf-size class kernels side by side + split-leaf sums",
-                  "traffic_bytes": 261.9e6 if default_cfg else None},
+                  "traffic_bytes": 59.0e6 * a.n / 262144 if default_cfg else None},
         "k_m2l": {"ms": per_step[5], "tflops": m2l_tf, "flops_per_launch": m2l_flops, "launches": 1,
                   "phase": "M2L (+ depth L2L launches, ~6 % of the phase)",
-                  "traffic_bytes": 265.4e6 if default_cfg else None},
+                  "traffic_bytes": 49.2e6 * stats["m2l_pairs"] / 11.21e6 if default_cfg else None},
     }
     dom = "k_m2l" if per_step[5] >= per_step[6] else "k_p2p"
     ach = kernels[dom]["tflops"]
     roofline = {"bound": "fp32-pipe", "achieved": ach, "peak": fp32_peak_tf, "unit": "TFLOP/s",
                 "frac": ach / fp32_peak_tf if fp32_peak_tf else None, "traffic": kernels[dom]["traffic_bytes"],
-                "traffic_unit": "bytes per step (ncu dram__bytes_read.sum + dram__bytes_write.sum)", "kernel": dom,
+                "traffic_unit": "bytes per step (ncu dram__bytes_read.sum + dram__bytes_write.sum of the kernel's "
+                                "launches, captured at N = 262,144 and scaled to N: profiles/)", "kernel": dom,
                 "peak_source": "FP32 FMA-chain microbenchmark on this GPU (nbody_measure_peaks); "
                                "MEASURED_PEAKS.json holds HBM and bf16 tensor peaks only",
                 "fp64_peak_tflops_measured": peaks[1] / 1e3,
