@@ -63,3 +63,43 @@ def test_static_direct_sum_rejects_oversize_requests(nb):
                                       None)
     assert rc == 1
     assert b"131072" in L.nbody_last_error(None)
+
+
+def test_static_direct_sum_limits_and_bad_targets_against_the_oracle(nb, oracle):
+    """The documented limits, on two calls in a row against the CPU oracle's FP64 direct sum (1e-12):
+    exactly 131,072 targets (indices repeated) are accepted; target indices outside [0, n) give NaN rows
+    and leave the other rows exact.  The calling thread's current device is the same afterwards."""
+    import torch
+    from nbody_gb300 import _lib, ics
+    L = _lib.load()
+    rng = np.random.default_rng(42)
+    pos, vel, m = ics.plummer(3000, seed=42)
+    n = len(m)
+    dev = torch.device("cuda", 0)
+    d_pos = torch.tensor(pos, dtype=torch.float64, device=dev).contiguous()
+    d_m = torch.tensor(m, dtype=torch.float64, device=dev)
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    before = torch.cuda.current_device()
+    for call, nt in enumerate((131072, 257)):
+        tg = rng.integers(0, n, nt).astype(np.int64)
+        bad = np.zeros(nt, bool)
+        if call == 1:
+            bad[[3, 100, 256]] = True
+            tg[bad] = [-1, n, 10 ** 12]
+        d_t = torch.tensor(tg, dtype=torch.int64, device=dev)
+        d_acc = torch.zeros((nt, 3), dtype=torch.float64, device=dev)
+        d_pot = torch.zeros((nt,), dtype=torch.float64, device=dev)
+        rc = L.nbody_direct_forces_static(0, n, _p(d_pos), _p(d_m), None, 0.01, 1.0, nt, _p(d_t), _p(d_acc),
+                                          _p(d_pot), stream)
+        assert rc == 0, L.nbody_last_error(None)
+        torch.cuda.synchronize(dev)
+        acc, pot = d_acc.cpu().numpy(), d_pot.cpu().numpy()
+        assert np.all(np.isnan(acc[bad])) and np.all(np.isnan(pot[bad]))
+        good = np.unique(tg[~bad])
+        a_ref, p_ref = oracle.direct(pos, m, m, eps=0.01, G=1.0, targets=good)
+        row = {t: k for k, t in enumerate(good)}
+        idx = np.array([row[t] for t in tg[~bad]])
+        err = np.linalg.norm(acc[~bad] - a_ref[idx], axis=1) / np.linalg.norm(a_ref[idx], axis=1)
+        assert err.max() < 1e-12, (call, err.max())
+        assert np.abs(pot[~bad] - p_ref[idx]).max() < 1e-12 * np.abs(p_ref).max()
+    assert torch.cuda.current_device() == before
