@@ -349,7 +349,7 @@ def main():
                            "loss sum(wx . x_N + wv . v_N), seeds and gradients resident on the device"}
         del out, wx, wv
 
-    # spec: the plain FP64 GPU FMM at equal accuracy, on the same initial conditions and time
+    # the target comparison: the plain FP64 GPU FMM at equal accuracy, on the same initial conditions and time
     # point (warm-up steps), the same order, for each leaf capacity tried; the fastest whose rms error
     # is within 5 % of the mixed form's (or at most 1e-4) is the comparator
     fp64_cmp = None

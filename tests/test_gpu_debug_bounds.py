@@ -1,7 +1,6 @@
 """The NBODY_DEBUG_BOUNDS build of the library (libnbody_gb300_debug.so).
 
-SURVEY-style race and bounds checking without compute-sanitizer: the debug
-build checks every index its kernels read from device data (the sorted-order
+Bounds checking without compute-sanitizer: the debug build checks every index its kernels read from device data (the sorted-order
 permutation, node ids of the pending, far-field and near-field lists, the
 particle ranges of near-field partners, radix-scatter destinations); an index
 out of range is replaced by an in-bounds one and reported as NBODY_ERR_CUDA at
