@@ -196,7 +196,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of each FP64 configuration")
     ap.add_argument("--drift-steps", type=int, default=1000,
                     help="leapfrog steps of the energy / momentum drift run from the initial state (0: skip)")
-    ap.add_argument("--block-K", type=int, default=0,
+    ap.add_argument("--block-K", type=int, default=3,
                     help="also time individual block steps with dt_max = dt * 2^K (0: skip)")
     ap.add_argument("--block-eta", type=float, default=0.02)
     a = ap.parse_args()
@@ -429,14 +429,20 @@ def main():
         torch.cuda.synchronize()
         ms_b = b0.elapsed_time(b1) / nbs
         st = sb.stats()
+        lv = np.bincount(sb.levels(), minlength=a.block_K + 1)
+        kfin = int(np.nonzero(lv)[0].max())            # finest level in use: the global step it would need
         block = {"K": a.block_K, "eta": a.block_eta, "dt_min": a.dt, "dt_max": a.dt * (1 << a.block_K),
                  "ms_per_base_step": ms_b, "fixed_ms_same_time": ms / a.steps * (1 << a.block_K),
                  "speedup_vs_fixed_dt_min": ms / a.steps * (1 << a.block_K) / ms_b,
-                 "levels": np.bincount(sb.levels(), minlength=a.block_K + 1).tolist(),
+                 "fixed_ms_at_finest_level_in_use": ms / a.steps * (1 << kfin),
+                 "speedup_vs_fixed_finest_level": ms / a.steps * (1 << kfin) / ms_b,
+                 "levels": lv.tolist(),
                  "near_field_leaves_evaluated_frac": st["block_active_leaves"] / max(st["block_leaves"], 1),
-                 "note": "time per base step of dt_max (2^K substeps, every particle drifted, forces evaluated "
-                         "on the whole tree, near field only for leaves with a particle closing its step) vs "
-                         "2^K fixed steps of dt_min"}
+                 "force_evaluations_per_base_step": st["block_evaluations"],
+                 "note": "time per base step of dt_max (2^K substeps, every particle drifted; forces evaluated "
+                         "on the whole tree at substeps where a step ends, near field only for leaves with a "
+                         "particle closing its step) vs 2^K fixed steps of dt_min, and vs the fixed step of the "
+                         "finest level in use (dt_max 2^-k, what one global step for all would need)"}
         sb.close()
 
     if rank != 0:

@@ -124,8 +124,9 @@ int nbody_set_timestep_control(nbody_ctx* c, int mode, double eta, double length
    (length <= 0: eps), chosen at the start of each of its steps from its
    acceleration there (a step may only start where the substep grid allows
    it), and receives its half kicks at the start and the end of each of its
-   steps.  Every substep evaluates all forces.  At the end of nbody_step all
-   particles are synchronous.  K = 0 is the fixed-step kick-drift-kick
+   steps.  A substep at which some step ends evaluates the forces (near
+   field only for leaves holding such a particle); the others only drift.
+   At the end of nbody_step all particles are synchronous.  K = 0 is the fixed-step kick-drift-kick
    leapfrog.  nbody_get_levels gives each particle's k (input order) of its
    last step; nbody_last_timestep returns dt_max. */
 int nbody_get_levels(nbody_ctx* c, int32_t* levels);
@@ -263,8 +264,9 @@ int nbody_direct_forces_static(int device, int64_t n, const double* pos, const d
    of the last step, out[7] evaluations since nbody_set_state whose fixed
    root box was grown (nbody_set_escape_policy), out[8] near-field leaves
    over the substeps of the last block step and out[9] how many of them
-   held a particle closing its step (the others' near field was skipped).
-   n = number of entries wanted (<= 10). */
+   held a particle closing its step (the others' near field was skipped),
+   out[10] the force evaluations of the last block step (substeps at which
+   no step can end only drift).  n = number of entries wanted (<= 11). */
 int nbody_get_stats(nbody_ctx* c, int64_t* out, int n);
 
 /* Floating-point operations this build counts per far-field cell pair

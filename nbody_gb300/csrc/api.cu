@@ -602,9 +602,10 @@ int nbody_diagnostics(nbody_ctx* c, double* out) {
 
 int nbody_get_stats(nbody_ctx* c, int64_t* out, int n) {
     if (!c || !out) return NBODY_ERR_INVALID;
-    const int64_t v[10] = {(int64_t)c->h_stats[0], (int64_t)c->h_stats[1], (int64_t)c->h_stats[2], c->nnodes,
-                           c->nleaves, c->depth, c->launches, c->escapes, c->blk_leaves, c->blk_active_leaves};
-    for (int i = 0; i < n && i < 10; ++i) out[i] = v[i];
+    const int64_t v[11] = {(int64_t)c->h_stats[0], (int64_t)c->h_stats[1], (int64_t)c->h_stats[2], c->nnodes,
+                           c->nleaves, c->depth, c->launches, c->escapes, c->blk_leaves, c->blk_active_leaves,
+                           c->blk_evals};
+    for (int i = 0; i < n && i < 11; ++i) out[i] = v[i];
     return NBODY_OK;
 }
 

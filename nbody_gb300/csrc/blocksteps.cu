@@ -10,8 +10,10 @@
 //              than the substep grid allows at s: k >= K - trailing_zeros(s)) and an opening half
 //              kick for its next step.
 // At the end of the base step every particle has closed its step, so positions and velocities are
-// synchronous again.  With K = 0 this is the kick-drift-kick leapfrog of one fixed step.  Every
-// substep evaluates the whole tree; the kicks are per particle, in fixed order, deterministic.
+// synchronous again.  With K = 0 this is the kick-drift-kick leapfrog of one fixed step.  A substep
+// at which some particle's step ends evaluates the whole tree, with the near field and L2P only for
+// the leaves holding such a particle; a substep at which none ends only drifts.  The kicks are per
+// particle, deterministic.
 #include "nbody_internal.cuh"
 
 namespace {
@@ -29,7 +31,8 @@ __device__ __forceinline__ int block_level(double a2, double eta, double len, do
 }
 
 // s = 0: levels and opening kicks of every particle; s >= 1: closing (and new opening) kicks of the
-// particles whose step ends at substep s
+// particles whose step ends at substep s.  ended[k] counts the closed steps of level k; ended[30]
+// (set to ~0 before the launch) receives the earliest substep after s at which a step ends.
 template <typename R>
 __global__ void __launch_bounds__(TB) k_block_kick(int64_t n, R* __restrict__ vx, R* __restrict__ vy,
                                                     R* __restrict__ vz, const R* __restrict__ ax,
@@ -38,28 +41,41 @@ __global__ void __launch_bounds__(TB) k_block_kick(int64_t n, R* __restrict__ vx
                                                     double dt_max, int K, int s, double eta, double len,
                                                     unsigned int* __restrict__ ended) {
     const int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t p = id[i];
-    const R a0 = ax[i], a1 = ay[i], a2 = az[i];
-    const double am2 = (double)a0 * (double)a0 + (double)a1 * (double)a1 + (double)a2 * (double)a2;
-    R v0 = vx[i], v1 = vy[i], v2 = vz[i];
-    if (s > 0) {
-        const int k = level[p];
-        if (s & ((1 << (K - k)) - 1)) return;          // its step does not end at this substep
-        const R h = (R)ldexp(dt_max, -(k + 1));
-        v0 += h * a0; v1 += h * a1; v2 += h * a2;
-        atomicAdd(&ended[k], 1u);
-        if (s == (1 << K)) {                           // end of the base step: synchronous again
+    unsigned int next = ~0u;                           // substep at which this particle's step ends
+    if (i < n) {
+        const uint32_t p = id[i];
+        const R a0 = ax[i], a1 = ay[i], a2 = az[i];
+        R v0 = vx[i], v1 = vy[i], v2 = vz[i];
+        bool opens = true;
+        if (s > 0) {
+            const int k = level[p];
+            const int span = 1 << (K - k);
+            if (s & (span - 1)) {                      // its step does not end at this substep
+                next = (unsigned int)((s / span + 1) * span);
+                opens = false;
+            } else {
+                const R h = (R)ldexp(dt_max, -(k + 1));
+                v0 += h * a0; v1 += h * a1; v2 += h * a2;
+                atomicAdd(&ended[k], 1u);
+                if (s == (1 << K)) {                   // end of the base step: synchronous again
+                    vx[i] = v0; vy[i] = v1; vz[i] = v2;
+                    opens = false;
+                }
+            }
+        }
+        if (opens) {
+            const double am2 = (double)a0 * (double)a0 + (double)a1 * (double)a1 + (double)a2 * (double)a2;
+            int k = block_level(am2, eta, len, dt_max, K);
+            if (s > 0) k = max(k, K - (__ffs(s) - 1));    // a new step must start on its own grid
+            level[p] = (uint8_t)k;
+            next = (unsigned int)(s + (1 << (K - k)));
+            const R h = (R)ldexp(dt_max, -(k + 1));
+            v0 += h * a0; v1 += h * a1; v2 += h * a2;
             vx[i] = v0; vy[i] = v1; vz[i] = v2;
-            return;
         }
     }
-    int k = block_level(am2, eta, len, dt_max, K);
-    if (s > 0) k = max(k, K - (__ffs(s) - 1));        // a new step must start on its own grid
-    level[p] = (uint8_t)k;
-    const R h = (R)ldexp(dt_max, -(k + 1));
-    v0 += h * a0; v1 += h * a1; v2 += h * a2;
-    vx[i] = v0; vy[i] = v1; vz[i] = v2;
+    next = __reduce_min_sync(0xffffffffu, next);
+    if ((threadIdx.x & 31) == 0 && next != ~0u) atomicMin(&ended[30], next);
 }
 
 // per leaf (near-field order): does one of its particles close its step at substep s?
@@ -84,6 +100,7 @@ template <typename R>
 int block_kick(nbody_ctx* c, int s) {
     const int k = c->cur;
     const double len = c->dt_len > 0.0 ? c->dt_len : c->prm.eps;
+    NB_CU(c, cudaMemsetAsync(DP<unsigned int>(c->blk_count) + 30, 0xff, sizeof(unsigned int), c->st));
     k_block_kick<R><<<nblk(c->n), TB, 0, c->st>>>(c->n, DP<R>(c->vx[k]), DP<R>(c->vy[k]), DP<R>(c->vz[k]),
                                                   DP<R>(c->ax[k]), DP<R>(c->ay[k]), DP<R>(c->az[k]),
                                                   DP<uint32_t>(c->id[k]), DP<uint8_t>(c->blk_level), c->dt_max,
@@ -118,13 +135,29 @@ int nb_block_step(nbody_ctx* c) {
     NB_TRY(c->rsz == 4 ? block_kick<float>(c, 0) : block_kick<double>(c, 0));
     const int S = 1 << c->blk_K;
     c->blk_leaves = 0;
+    c->blk_evals = 0;
+    int next = 0;
     for (int s = 1; s <= S; ++s) {
+        if (s > next) {
+            // the earliest substep at which a step ends, from the last kick (at most S: every step
+            // ends by the end of the base step)
+            NB_CU(c, cudaMemcpyAsync(&c->h_blk_count[30], DP<unsigned int>(c->blk_count) + 30,
+                                     sizeof(unsigned int), cudaMemcpyDeviceToHost, c->st));
+            NB_CU(c, cudaStreamSynchronize(c->st));
+            next = (int)c->h_blk_count[30];
+            if (next < s || next > S) return nb_fail(c, NBODY_ERR_STATE, "block step: bad next substep");
+        }
+        if (s < next) {
+            NB_TRY(nb_drift(c, c->blk_dt));          // no particle's step ends here: drift only
+            continue;
+        }
         // drift of every particle + forces; near field and L2P only for leaves holding a particle whose
         // step ends at s (the others' accelerations are not used at this substep)
         c->blk_s = s;
         const int rc = nb_evaluate(c, 2, NB_INTEG_NONE, false);
         c->blk_s = 0;
         NB_TRY(rc);
+        ++c->blk_evals;
         NB_TRY(c->rsz == 4 ? block_kick<float>(c, s) : block_kick<double>(c, s));
     }
     NB_CU(c, cudaMemcpyAsync(c->h_blk_count, c->blk_count.p, sizeof(unsigned int) * 32, cudaMemcpyDeviceToHost, c->st));

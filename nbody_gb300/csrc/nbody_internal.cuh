@@ -201,6 +201,7 @@ struct nbody_ctx {
     DevBuf blk_count;              // per level: closing kicks of the last base step
     DevBuf blk_active;             // per leaf (near-field order): a particle closes its step at substep blk_s
     int blk_s = 0;                 // substep of the evaluation in progress (0: not a block substep)
+    int64_t blk_evals = 0;         // force evaluations of the last block step (substeps where a step ended)
     int64_t blk_leaves = 0, blk_active_leaves = 0;   // near-field leaves evaluated vs skipped (stats)
     unsigned int h_blk_count[32] = {0};
     double amax2 = 0;
@@ -252,6 +253,7 @@ int nb_download_state(nbody_ctx* c, int order);
 
 // tree (tree.cu)
 int nb_kick_drift(nbody_ctx* c);
+int nb_drift(nbody_ctx* c, double dt);
 int nb_begin_step(nbody_ctx* c, int kdk);
 int nb_sort_and_gather(nbody_ctx* c);
 int nb_build_tree(nbody_ctx* c);

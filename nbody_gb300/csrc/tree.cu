@@ -417,6 +417,23 @@ int nb_kick_drift(nbody_ctx* c) {
     return NBODY_OK;
 }
 
+// drift of the current state buffer by dt, nothing else (block steps: substeps without a kick)
+int nb_drift(nbody_ctx* c, double dt) {
+    unsigned g = nblk(c->n);
+    if (g > 152 * 8) g = 152 * 8;
+    if (g == 0) g = 1;
+    unsigned long long* bb = DP<unsigned long long>(c->bbox);
+    if (c->rsz == 4)
+        k_kick_drift_bbox<float><<<g, TB, 0, c->st>>>(c->n, state<float>(c, c->cur), 0.5 * dt, dt, 2, bb,
+                                                      DP<int32_t>(c->info));
+    else
+        k_kick_drift_bbox<double><<<g, TB, 0, c->st>>>(c->n, state<double>(c, c->cur), 0.5 * dt, dt, 2, bb,
+                                                       DP<int32_t>(c->info));
+    NB_LAUNCHED(c, "drift");
+    c->launches += 1;
+    return NBODY_OK;
+}
+
 int nb_sort_and_gather(nbody_ctx* c) {
     int first = 1;
     NB_TRY(nb_radix_sort(c, c->n, DP<uint64_t>(c->keys[0]), DP<uint32_t>(c->vals[0]), DP<uint64_t>(c->keys[1]),

@@ -280,10 +280,10 @@ class CudaSimulation:
         return cur.value, peak.value
 
     def stats(self):
-        out = np.zeros(10, np.int64)
-        check(self._h, _lib.load().nbody_get_stats(self._h, ptr(out), 10))
+        out = np.zeros(11, np.int64)
+        check(self._h, _lib.load().nbody_get_stats(self._h, ptr(out), 11))
         keys = ("m2l_pairs", "p2p_particle_pairs", "p2p_leaf_pairs", "nodes", "leaves", "depth", "launches",
-                "grown_boxes", "block_leaves", "block_active_leaves")
+                "grown_boxes", "block_leaves", "block_active_leaves", "block_evaluations")
         return dict(zip(keys, (int(v) for v in out)))
 
     def set_escape_policy(self, policy: str = "grow"):

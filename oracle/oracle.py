@@ -351,12 +351,14 @@ def block_level(acc, eta, length, dt_max, K):
     return k
 
 
-def leapfrog_block(pos, vel, q, m, eps, G, eta, length, dt_max, K, steps, nthreads=None):
+def leapfrog_block(pos, vel, q, m, eps, G, eta, length, dt_max, K, steps, nthreads=None, stats=None):
     """FP64 direct-sum kick-drift-kick leapfrog with individual power-of-two steps (the library's
     NBODY_DT_BLOCK scheme): per base step dt_max, 2^K substeps of dt_max 2^-K; every particle drifts
     every substep; a particle's step of dt_max 2^-k starts with a half kick and ends with one, and
     its level comes from block_level at the start of each of its steps, no coarser than the substep
-    grid allows there.  Returns (pos, vel, acc, levels of the last steps)."""
+    grid allows there.  Returns (pos, vel, acc, levels of the last steps).  With a dict `stats`,
+    stats["evaluations"] = substeps of the last base step at which some particle's step ended (the
+    ones that need forces)."""
     x = np.array(pos, dtype=np.float64).reshape(-1, 3)
     v = np.array(vel, dtype=np.float64).reshape(-1, 3)
     length = length if length > 0.0 else eps
@@ -366,16 +368,20 @@ def leapfrog_block(pos, vel, q, m, eps, G, eta, length, dt_max, K, steps, nthrea
     for _ in range(steps):
         lv = block_level(a, eta, length, dt_max, K)
         v = v + np.ldexp(dt_max, -(lv + 1))[:, None] * a
+        evaluations = 0
         for s in range(1, S + 1):
             x = x + np.ldexp(dt_max, -K) * v
             a = direct(x, q, m, eps, G, nthreads=nthreads)[0]
             end = (s & ((1 << (K - lv)) - 1)) == 0
+            evaluations += bool(end.any())
             v = v + np.where(end, np.ldexp(dt_max, -(lv + 1)), 0.0)[:, None] * a
             if s < S:
                 tz = (s & -s).bit_length() - 1
                 new = np.maximum(block_level(a, eta, length, dt_max, K), K - tz)
                 lv = np.where(end, new, lv)
                 v = v + np.where(end, np.ldexp(dt_max, -(lv + 1)), 0.0)[:, None] * a
+        if stats is not None:
+            stats["evaluations"] = evaluations
     return x, v, a, lv
 
 

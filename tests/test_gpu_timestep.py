@@ -96,11 +96,13 @@ def test_block_steps_match_fp64_direct(nb, oracle):
     assert sim.time == pytest.approx(steps * dt_max, rel=1e-14, abs=0)
     lv = sim.levels()
     p1, v1, _, _, _ = sim.state("input")
-    p2, v2, _, lv2 = oracle.leapfrog_block(pos, vel, m, m, 0.01, 1.0, eta, 0.0, dt_max, 3, steps)
+    ost = {}
+    p2, v2, _, lv2 = oracle.leapfrog_block(pos, vel, m, m, 0.01, 1.0, eta, 0.0, dt_max, 3, steps, stats=ost)
     np.testing.assert_array_equal(lv, lv2)
     assert len(np.unique(lv)) >= 2, np.bincount(lv)
     st = sim.stats()                      # some substeps skipped the near field of some leaves
     assert 0 < st["block_active_leaves"] < st["block_leaves"], st
+    assert st["block_evaluations"] == ost["evaluations"], (st, ost)
     assert np.abs(p1 - p2).max() < 1e-7
     assert np.abs(v1 - v2).max() < 1e-5
     # the recorded run of the adjoint refuses block steps; back to the fixed step
@@ -110,6 +112,28 @@ def test_block_steps_match_fp64_direct(nb, oracle):
     sim.step()
     assert sim.last_timestep() == 1e-3
     sim.close()
+
+
+def test_block_substeps_without_an_ending_step_only_drift(nb):
+    """K = 3 with every particle on level 0 (a large eta): one force evaluation per base step, at its
+    end; the other seven substeps only drift.  The result is the fixed leapfrog step of dt_max with
+    its drift taken in eight parts: equal to a few ulps."""
+    pos, vel, m = ics.plummer(2048, seed=66)
+    a = _sim(nb, pos, vel, m, order=6, leaf_capacity=16, dt=8e-3)
+    a.step(2)
+    b = _sim(nb, pos, vel, m, order=6, leaf_capacity=16, dt=8e-3)
+    b.set_timestep_control("block", eta=1e6, length=0.0, dt_min=1e-3, dt_max=8e-3)
+    b.step(2)
+    assert np.all(b.levels() == 0)
+    st = b.stats()
+    assert st["block_evaluations"] == 1, st
+    assert st["block_active_leaves"] == st["block_leaves"] == st["leaves"], st
+    pa, va = a.state("input")[:2]
+    pb, vb = b.state("input")[:2]
+    np.testing.assert_allclose(pb, pa, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(vb, va, rtol=0, atol=1e-12)
+    a.close()
+    b.close()
 
 
 def test_block_steps_with_one_level_are_the_fixed_leapfrog(nb):

@@ -355,8 +355,16 @@ def test_block_leapfrog_reduces_to_the_fixed_step(oracle):
     np.testing.assert_allclose(x1, x0, rtol=0, atol=1e-14)
     np.testing.assert_allclose(v1, v0, rtol=0, atol=1e-13)
     assert np.all(lv == 0)
-    x2, v2, a2, lv2 = oracle.leapfrog_block(pos, vel, m, m, 0.01, 1.0, 0.02, 0.0, 8e-3, 3, 2)
+    st = {}
+    x2, v2, a2, lv2 = oracle.leapfrog_block(pos, vel, m, m, 0.01, 1.0, 0.02, 0.0, 8e-3, 3, 2, stats=st)
     assert np.all((lv2 >= 0) & (lv2 <= 3)) and len(np.unique(lv2)) >= 2
+    # forces are needed at a substep only where some step ends: 2^(deepest level) of the 8 at most
+    assert 1 <= st["evaluations"] <= 8
+    if lv2.max() < 3:
+        assert st["evaluations"] < 8
+    st1 = {}
+    oracle.leapfrog_block(pos, vel, m, m, 0.01, 1.0, 1e6, 0.0, 8e-3, 3, 1, stats=st1)
+    assert st1["evaluations"] == 1                 # every particle on level 0: only the last substep
     # a finer global step moves toward the block result more than the coarse one does
     xf, _, _ = oracle.leapfrog(pos, vel, m, m, 0.01, 1.0, 1e-3, 16)
     xc, _, _ = oracle.leapfrog(pos, vel, m, m, 0.01, 1.0, 8e-3, 2)
