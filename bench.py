@@ -190,7 +190,9 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=20, help="steps of the timed forward+adjoint runs (0: skip)")
     ap.add_argument("--adj-every", type=int, default=20,
                     help="checkpoint spacing of the headline forward+adjoint run (recomputation inside each "
-                         "segment); a second run keeps every evaluation (spacing 0)")
+                         "segment but the last); a second run keeps every evaluation (spacing 0)")
+    ap.add_argument("--adj-every-multi", type=int, default=5,
+                    help="checkpoint spacing of a third run with several segments (0: skip)")
     ap.add_argument("--fp64-caps", default="64,32",
                     help="leaf capacities tried for the plain FP64 GPU FMM at the same order ('' to skip)")
     ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of each FP64 configuration")
@@ -324,6 +326,15 @@ def main():
         rec_peak = sim.device_memory()[1]
         adj_ms = timed_fwd_bwd(a.adj_every)
         fin = all(bool(torch.isfinite(t).all()) for t in out)
+        multi = None
+        if 0 < a.adj_every_multi < a.adj_steps:
+            multi_ms = timed_fwd_bwd(a.adj_every_multi)
+            nseg = (a.adj_steps + a.adj_every_multi - 1) // a.adj_every_multi
+            multi = {"ms_per_step": multi_ms / a.adj_steps, "checkpoint_every": a.adj_every_multi,
+                     "segments": nseg, "cost_vs_forward_step": multi_ms / a.adj_steps / fwd_ms,
+                     "gradients_finite": all(bool(torch.isfinite(t).all()) for t in out),
+                     "note": "the same run with several checkpoint segments: all but the last recomputed "
+                             "forward by the reverse sweep"}
         fwd_adj_rec = {"value": a.n * a.adj_steps * world / (rec_ms * 1e-3), "unit": UNIT,
                        "ms_per_step": rec_ms / a.adj_steps, "steps": a.adj_steps, "checkpoint_every": 0,
                        "cost_vs_forward_step": rec_ms / a.adj_steps / fwd_ms, "gradients_finite": fin_rec,
@@ -341,10 +352,11 @@ def main():
                    "ms_per_step": adj_ms / a.adj_steps, "steps": a.adj_steps, "checkpoint_every": a.adj_every,
                    "cost_vs_forward_step": adj_ms / a.adj_steps / fwd_ms,
                    "gradients_finite": fin, "vjp_phase_ms": vjp_ph, "vjp_launches": vjp_launches,
-                   "recorded_every_evaluation": fwd_adj_rec,
+                   "recorded_every_evaluation": fwd_adj_rec, "several_segments": multi,
                    "note": "one leapfrog run of `steps` steps with a sorted-state checkpoint every "
                            "`checkpoint_every` steps, plus its reverse sweep (frozen-tree discrete adjoint: "
-                           "each segment recomputed forward from its checkpoint, one force VJP per time point); "
+                           "each segment recomputed forward from its checkpoint, except the last, which the "
+                           "forward run records as it goes; one force VJP per time point); "
                            "cost_vs_forward_step = (forward + adjoint ms per step) / forward ms per step; "
                            "loss sum(wx . x_N + wv . v_N), seeds and gradients resident on the device"}
         del out, wx, wv

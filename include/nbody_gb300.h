@@ -181,7 +181,9 @@ int nbody_force_vjp(nbody_ctx* c, const double* mu, double* gx, double* gq, doub
    only: the snapshot holds its accelerations; then every - 1 full steps) and
    records those evaluations whole, so it holds the records of one interval
    (about 370 bytes per particle per time point at order 5 and leaf capacity
-   64) while it runs.
+   64).  The last interval, the first one the reverse sweep needs, is
+   recorded by this call as it runs and is not recomputed, so this call
+   already holds those records.
    every = 0: every time point's whole evaluation (tree, lists, local
    expansions, particle offsets), so the reverse sweep evaluates nothing:
    about 370 bytes per particle per time point at order 5 and leaf capacity

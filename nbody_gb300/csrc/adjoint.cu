@@ -14,9 +14,10 @@
 // snapshot already holds the accelerations: its far field only is evaluated)
 // and every evaluation of the segment is recorded whole, so the segment's
 // reverse pass re-evaluates nothing; memory: one snapshot per checkpoint plus
-// the records of one segment.  Snapshots hold the sorted state (positions,
-// velocities, accelerations, masses, charges, ids), so a recomputed segment
-// is bitwise the recorded one.
+// the records of one segment.  The last segment, the first one the reverse
+// sweep needs, is recorded during the forward run itself and not recomputed.
+// Snapshots hold the sorted state (positions, velocities, accelerations,
+// masses, charges, ids), so a recomputed segment is bitwise the recorded one.
 #include <algorithm>
 
 #include "nbody_internal.cuh"
@@ -214,9 +215,13 @@ int rec_save(nbody_ctx* c, int j) {
 }
 
 // makes record j the context's current evaluation (the particle state arrays it includes are the
-// sorted charges, masses, accelerations and ids; positions and velocities are left alone)
+// sorted charges, masses, accelerations and ids; positions and velocities are left alone); the
+// tree is then the record's, neither the current state's nor the recorded run's final one until a
+// caller says so
 int rec_load(nbody_ctx* c, int j) {
     EvalRecord& R = c->recs[j];
+    c->eval_current = false;
+    c->tree_at_final = false;
     RecField f[24] = {};
     const int nf = rec_fields(c, R.nn, R.nl, (uint32_t)R.info[INFO_M2L_TAIL], (uint32_t)R.info[INFO_P2P_TAIL], f);
     size_t o = 0;
@@ -287,23 +292,32 @@ int nbody_forward_checkpointed(nbody_ctx* c, int nsteps, int every, double* t_ou
     c->snap_bytes = snapshot_bytes(c);
     const int slots = rec ? 1 : (nsteps + every - 1) / every + 1;
     NB_TRY(nb_grow(c, c->snaps, c->snap_bytes * (size_t)slots));
-    // time point 0 needs its accelerations, and in record mode its whole evaluation
-    if (!c->have_acc || (rec && !c->eval_current)) {
+    // first time point of the last checkpoint interval: its evaluations are recorded as they happen
+    const int s_last = rec ? 0 : ((nsteps - 1) / every) * every;
+    c->ck_last_recorded = false;
+    // time point 0 needs its accelerations, and its whole evaluation where it is recorded (the far
+    // field only where the accelerations are known, as the reverse sweep's recomputation does)
+    if (!c->have_acc) {
         NB_TRY(nb_evaluate(c, 0, NB_INTEG_NONE, false));
         c->have_acc = true;
+    } else if (s_last == 0 && !c->eval_current) {
+        NB_TRY(nb_evaluate(c, 0, rec ? NB_INTEG_NONE : NB_INTEG_FAR_ONLY, false));
     }
     c->ck_t0 = c->time;
     c->ck_every = every;
     c->ck_steps = nsteps;
     if (rec) NB_TRY(rec_save(c, 0));
     else NB_TRY(snap_save(c, 0));
+    if (!rec && s_last == 0) NB_TRY(rec_save(c, 0));
     for (int s = 0; s < nsteps; ++s) {
         NB_TRY(nb_evaluate(c, 1, NB_INTEG_KDK_CLOSE, false));
         c->time += c->prm.dt;
         const int pt = s + 1;
         if (rec) NB_TRY(rec_save(c, pt));
         else if (pt < nsteps && pt % every == 0) NB_TRY(snap_save(c, pt / every));
+        if (!rec && pt >= s_last && pt < nsteps) NB_TRY(rec_save(c, pt - s_last));
     }
+    c->ck_last_recorded = !rec;
     NB_TRY(snap_save(c, final_slot(c)));
     NB_CU(c, cudaStreamSynchronize(c->st));
     c->tree_at_final = true;
@@ -427,23 +441,32 @@ int nbody_backward(nbody_ctx* c, const double* gxT, const double* gvT, double* g
     NB_TRY(vjp(c, 0.5 * dt));
     // segments [s0, e), last first: the checkpoint's tree, lists and far field (its snapshot holds
     // the accelerations), then the recomputed steps s0+1 .. e-1, each evaluation recorded whole, so
-    // the segment's reverse pass re-evaluates nothing
-    for (int s0 = ((N - 1) / every) * every; s0 >= 0; s0 -= every) {
+    // the segment's reverse pass re-evaluates nothing.  The last segment's records come from the
+    // forward run, as long as no earlier segment has been recomputed over them since.
+    const int s_last = ((N - 1) / every) * every;
+    for (int s0 = s_last; s0 >= 0; s0 -= every) {
         const int e = std::min(s0 + every, N);
-        NB_TRY(snap_load(c, s0 / every));
-        c->time = c->ck_t0 + s0 * dt;
-        NB_TRY(nb_evaluate(c, 0, NB_INTEG_FAR_ONLY, false));
-        NB_TRY(rec_save(c, 0));
-        for (int pt = s0 + 1; pt <= e - 1; ++pt) {
-            NB_TRY(nb_evaluate(c, 1, NB_INTEG_KDK_CLOSE, false));
-            NB_TRY(rec_save(c, pt - s0));
+        const bool recorded = s0 == s_last && c->ck_last_recorded;
+        if (!recorded) {
+            c->ck_last_recorded = false;
+            NB_TRY(snap_load(c, s0 / every));
+            c->time = c->ck_t0 + s0 * dt;
+            NB_TRY(nb_evaluate(c, 0, NB_INTEG_FAR_ONLY, false));
+            NB_TRY(rec_save(c, 0));
+            for (int pt = s0 + 1; pt <= e - 1; ++pt) {
+                NB_TRY(nb_evaluate(c, 1, NB_INTEG_KDK_CLOSE, false));
+                NB_TRY(rec_save(c, pt - s0));
+            }
         }
         for (int pt = e - 1; pt >= s0; --pt) {
             NB_TRY(rev_drift(c));
-            if (pt < e - 1) NB_TRY(rec_load(c, pt - s0));     // pt = e - 1 is the current evaluation
+            // after a recomputation, pt = e - 1 is the current evaluation
+            if (recorded || pt < e - 1) NB_TRY(rec_load(c, pt - s0));
             NB_TRY(vjp(c, pt == 0 ? 0.5 * dt : dt));
         }
     }
+    // the records hold the last segment again only if it was the only one
+    c->ck_last_recorded = s_last == 0;
     NB_TRY(download_r(c, c->adj_lx, 3 * n, gx0, st));
     NB_TRY(download_r(c, c->adj_lv, 3 * n, gv0, st + 3 * n));
     NB_TRY(download_r(c, c->adj_gq, n, gq, st + 6 * n));

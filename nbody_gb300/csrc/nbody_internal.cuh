@@ -174,6 +174,7 @@ struct nbody_ctx {
     double ck_t0 = 0.0;            // simulated time at its start
     bool tree_at_final = false;    // the last evaluation was the recorded run's final one
     bool rec_mode = false;         // the recorded run kept every evaluation (no re-evaluation backward)
+    bool ck_last_recorded = false; // records hold the last checkpoint interval of the recorded run
     bool eval_current = false;     // tree, lists and expansions match the current state
     bool lists_frozen = false;     // the force evaluation reuses the loaded lists (frozen-structure replay)
     std::vector<EvalRecord> recs;  // its evaluations, time points 0 .. steps

@@ -134,6 +134,21 @@ def test_checkpoint_spacing_gives_identical_gradients(nb, prec):
             np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("every", [2, 7])
+def test_second_backward_equals_the_first(nb, every):
+    """The last checkpoint interval is recorded by the forward run and not recomputed by the first
+    reverse sweep; a second reverse sweep over the same run (whose records the first one replaced
+    with the earlier intervals' when there are several) gives the same gradients bitwise."""
+    pos, vel, m = ics.clustered(3000, seed=46)
+    rng = np.random.default_rng(10)
+    gxT, gvT = rng.normal(size=pos.shape), rng.normal(size=pos.shape)
+    g1, sim = _run(nb, pos, vel, m, "mixed", 5, 7, every, gxT, gvT)
+    g2 = sim.backward(gxT, gvT)
+    for a, b in zip(g1, g2):
+        np.testing.assert_array_equal(a, b)
+    sim.close()
+
+
 def test_backward_needs_a_recorded_run(nb):
     pos, vel, m = ics.plummer(500, seed=45)
     sim = _sim(nb, pos, vel, m, m, "mixed", 3, integrator=nb.INTEG_LEAPFROG)
