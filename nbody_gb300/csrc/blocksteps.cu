@@ -32,7 +32,9 @@ __device__ __forceinline__ int block_level(double a2, double eta, double len, do
 
 // s = 0: levels and opening kicks of every particle; s >= 1: closing (and new opening) kicks of the
 // particles whose step ends at substep s.  ended[k] counts the closed steps of level k; ended[30]
-// (set to ~0 before the launch) receives the earliest substep after s at which a step ends.
+// (set to ~0 before the launch) receives the earliest substep after s at which a step ends.  Both
+// are gathered per block in shared memory first: one global atomic per level and block, not one
+// per particle on the same word.
 template <typename R>
 __global__ void __launch_bounds__(TB) k_block_kick(int64_t n, R* __restrict__ vx, R* __restrict__ vy,
                                                     R* __restrict__ vz, const R* __restrict__ ax,
@@ -40,6 +42,11 @@ __global__ void __launch_bounds__(TB) k_block_kick(int64_t n, R* __restrict__ vx
                                                     const uint32_t* __restrict__ id, uint8_t* __restrict__ level,
                                                     double dt_max, int K, int s, double eta, double len,
                                                     unsigned int* __restrict__ ended) {
+    __shared__ unsigned int s_ended[32];
+    __shared__ unsigned int s_next;
+    if (threadIdx.x < 32) s_ended[threadIdx.x] = 0;
+    if (threadIdx.x == 0) s_next = ~0u;
+    __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * TB + threadIdx.x;
     unsigned int next = ~0u;                           // substep at which this particle's step ends
     if (i < n) {
@@ -56,7 +63,7 @@ __global__ void __launch_bounds__(TB) k_block_kick(int64_t n, R* __restrict__ vx
             } else {
                 const R h = (R)ldexp(dt_max, -(k + 1));
                 v0 += h * a0; v1 += h * a1; v2 += h * a2;
-                atomicAdd(&ended[k], 1u);
+                atomicAdd(&s_ended[k], 1u);
                 if (s == (1 << K)) {                   // end of the base step: synchronous again
                     vx[i] = v0; vy[i] = v1; vz[i] = v2;
                     opens = false;
@@ -75,25 +82,42 @@ __global__ void __launch_bounds__(TB) k_block_kick(int64_t n, R* __restrict__ vx
         }
     }
     next = __reduce_min_sync(0xffffffffu, next);
-    if ((threadIdx.x & 31) == 0 && next != ~0u) atomicMin(&ended[30], next);
+    if ((threadIdx.x & 31) == 0 && next != ~0u) atomicMin(&s_next, next);
+    __syncthreads();
+    if (threadIdx.x <= (unsigned)K && s_ended[threadIdx.x]) atomicAdd(&ended[threadIdx.x], s_ended[threadIdx.x]);
+    if (threadIdx.x == 0 && s_next != ~0u) atomicMin(&ended[30], s_next);
 }
 
-// per leaf (near-field order): does one of its particles close its step at substep s?
+// per leaf (near-field order), one warp each: does one of its particles close its step at substep
+// s?  32 particles' levels per load round; the active leaves are counted per block, then globally.
 __global__ void __launch_bounds__(TB) k_block_active(int64_t nleaves, const uint32_t* __restrict__ leaves,
                                                       const NodeRec* __restrict__ nodes,
                                                       const uint32_t* __restrict__ id,
                                                       const uint8_t* __restrict__ level, int K, int s,
                                                       uint8_t* __restrict__ active, unsigned int* __restrict__ count) {
-    const int64_t li = (int64_t)blockIdx.x * TB + threadIdx.x;
-    if (li >= nleaves) return;
-    const NodeRec nd = nodes[leaves[li]];
-    uint8_t a = 0;
-    for (uint32_t i = nd.begin; i < nd.begin + nd.count && !a; ++i) {
-        const int k = level[id[i]];
-        a = (s & ((1 << (K - k)) - 1)) == 0;
+    __shared__ unsigned int s_count;
+    if (threadIdx.x == 0) s_count = 0;
+    __syncthreads();
+    const int64_t li = (int64_t)blockIdx.x * (TB / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (li < nleaves) {                                // warp-uniform
+        const NodeRec nd = nodes[leaves[li]];
+        bool a = false;
+        for (uint32_t b = 0; b < nd.count && !a; b += 32) {
+            bool mine = false;
+            if (b + lane < nd.count) {
+                const int k = level[id[nd.begin + b + lane]];
+                mine = (s & ((1 << (K - k)) - 1)) == 0;
+            }
+            a = __any_sync(0xffffffffu, mine);
+        }
+        if (lane == 0) {
+            active[li] = a;
+            if (a) atomicAdd(&s_count, 1u);
+        }
     }
-    active[li] = a;
-    if (a) atomicAdd(count, 1u);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_count) atomicAdd(count, s_count);
 }
 
 template <typename R>
@@ -113,7 +137,7 @@ int block_kick(nbody_ctx* c, int s) {
 
 int nb_block_active_leaves(nbody_ctx* c) {
     NB_TRY(nb_grow(c, c->blk_active, (size_t)c->nleaves + 1));
-    k_block_active<<<nblk(c->nleaves), TB, 0, c->st>>>(c->nleaves, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes),
+    k_block_active<<<(unsigned)((c->nleaves + TB / 32 - 1) / (TB / 32)), TB, 0, c->st>>>(c->nleaves, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes),
                                                        DP<uint32_t>(c->id[c->cur]), DP<uint8_t>(c->blk_level),
                                                        c->blk_K, c->blk_s, DP<uint8_t>(c->blk_active),
                                                        DP<unsigned int>(c->blk_count) + 31);
