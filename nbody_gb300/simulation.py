@@ -208,8 +208,9 @@ class CudaSimulation:
         return gx, gq, gm
 
     def forward_checkpointed(self, nsteps: int, every: int = 1) -> float:
-        """nsteps leapfrog steps recorded for backward(): snapshots every `every` steps, or with every = 0
-        every time point's whole evaluation (no re-evaluation in the reverse sweep)."""
+        """nsteps leapfrog steps recorded for backward(): snapshots every `every` steps (the last interval's
+        evaluations are kept whole as they happen, the reverse sweep recomputes the earlier intervals),
+        or with every = 0 every time point's whole evaluation (no re-evaluation in the reverse sweep)."""
         t = C.c_double()
         check(self._h, _lib.load().nbody_forward_checkpointed(self._h, int(nsteps), int(every), C.byref(t)))
         return t.value
@@ -280,6 +281,9 @@ class CudaSimulation:
         return cur.value, peak.value
 
     def stats(self):
+        """Work counts of the last evaluation (pairs, nodes, leaves, depth, launches), evaluations that
+        took a grown root box, and of the last block step: leaves over its evaluated substeps, those
+        whose near field ran, and its force evaluations."""
         out = np.zeros(11, np.int64)
         check(self._h, _lib.load().nbody_get_stats(self._h, ptr(out), 11))
         keys = ("m2l_pairs", "p2p_particle_pairs", "p2p_leaf_pairs", "nodes", "leaves", "depth", "launches",
