@@ -30,8 +30,8 @@
  *   5. The reference order-0 FMM restated in FP32 arithmetic following
  *      src/field.cl:17-47 (pair and node fields), src/force.cl:21-81
  *      (F = q * sum of fields) and src/open_cl_simulation.cpp:600-607
- *      (explicit Euler: v += F/m dt, x += v_old dt), with the reference bugs
- *      listed in the survey fixed (M2M runs, interaction slots are distinct,
+ *      (explicit Euler: v += F/m dt, x += v_old dt), with four bugs of the
+ *      reference's host code fixed (M2M runs, interaction slots are distinct,
  *      the leaf partition covers every leaf, every batch is integrated).
  *   6. FP64 softened direct sum (forces and potential) and its adjoint.
  *   7. A port of src/naive_simulation.cpp:7-46 (the reference CPU path), with
