@@ -48,6 +48,18 @@ def dist_env():
     return rank, world, local
 
 
+def rank_max(x, device="cuda"):
+    """The largest x over the ranks of the default process group (x itself without one): every timed
+    figure of a multi-rank run is the slowest rank's."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload_desc(a):
     return {
         "workload": f"collision1m: N={a.n:,} two Plummer spheres (a=1, M=0.5 each, 10a apart on x, impact 1a, "
@@ -253,11 +265,7 @@ def main():
     wall = time.perf_counter() - w0
     clk = clocks.stop()
     sim.set_timing(False)
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = rank_max(ev0.elapsed_time(ev1))
     value = a.n * a.steps * world / (ms * 1e-3)
 
     # end to end through the C ABI with pinned host buffers
@@ -284,11 +292,7 @@ def main():
     for _ in range(a.e2e_steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - e0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = rank_max(time.perf_counter() - e0)
     e2e = a.n * a.e2e_steps * world / e2e_s
 
     # forward + adjoint: a recorded run of adj_steps steps and its reverse sweep, with the loss
@@ -320,12 +324,7 @@ def main():
             fwd_bwd(a.adj_steps, every)
             eb.record(stream)
             torch.cuda.synchronize()
-            t_ms = ea.elapsed_time(eb)
-            if world > 1:
-                t = torch.tensor([t_ms], device="cuda")
-                torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-                t_ms = float(t.item())
-            return t_ms
+            return rank_max(ea.elapsed_time(eb))
 
         fwd_ms = ms / a.steps
         rec_ms = timed_fwd_bwd(0)
