@@ -137,10 +137,10 @@ int block_kick(nbody_ctx* c, int s) {
 
 int nb_block_active_leaves(nbody_ctx* c) {
     NB_TRY(nb_grow(c, c->blk_active, (size_t)c->nleaves + 1));
-    k_block_active<<<(unsigned)((c->nleaves + TB / 32 - 1) / (TB / 32)), TB, 0, c->st>>>(c->nleaves, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes),
-                                                       DP<uint32_t>(c->id[c->cur]), DP<uint8_t>(c->blk_level),
-                                                       c->blk_K, c->blk_s, DP<uint8_t>(c->blk_active),
-                                                       DP<unsigned int>(c->blk_count) + 31);
+    const unsigned grid = (unsigned)((c->nleaves + TB / 32 - 1) / (TB / 32));     // a warp per leaf
+    k_block_active<<<grid, TB, 0, c->st>>>(c->nleaves, DP<uint32_t>(c->leaves), DP<NodeRec>(c->nodes),
+                                           DP<uint32_t>(c->id[c->cur]), DP<uint8_t>(c->blk_level), c->blk_K,
+                                           c->blk_s, DP<uint8_t>(c->blk_active), DP<unsigned int>(c->blk_count) + 31);
     NB_LAUNCHED(c, "block active leaves");
     c->launches += 1;
     c->blk_leaves += c->nleaves;
