@@ -205,6 +205,18 @@ def test_derivative_recursion_matches_oracle(oracle):
         np.testing.assert_allclose(D, Dref, rtol=1e-12, atol=1e-14 * np.abs(Dref).max())
 
 
+def test_generated_operators_are_current():
+    """csrc/fmm_ops.inc is the output of csrc/gen_ops.py, byte for byte (the build regenerates it only
+    when the generator is newer, so a stale committed copy would go unnoticed)."""
+    import os
+    import subprocess
+    import sys
+    csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "nbody_gb300", "csrc")
+    out = subprocess.run([sys.executable, os.path.join(csrc, "gen_ops.py")], capture_output=True, check=True).stdout
+    with open(os.path.join(csrc, "fmm_ops.inc"), "rb") as f:
+        assert f.read() == out
+
+
 def test_initial_conditions_are_seeded_and_sane():
     a = ics.plummer(2000, seed=3)
     b = ics.plummer(2000, seed=3)
