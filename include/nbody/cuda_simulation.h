@@ -210,6 +210,13 @@ public:
         check(nbody_last_timestep(_ctx, &dt), "nbody_last_timestep");
         return dt;
     }
+    /* block steps: each particle's level k (its last step was dtMax / 2^k), in the order particles were
+       given to the constructor */
+    std::vector<int32_t> levels() const {
+        std::vector<int32_t> k((size_t)_n);
+        check(nbody_get_levels(_ctx, k.data()), "nbody_get_levels");
+        return k;
+    }
 
     /* particles leaving the fixed root box [0, bounds): NBODY_ESCAPE_GROW (default) steps on the
        smallest grown box that keeps [0, bounds) as one of its cells, NBODY_ESCAPE_ERROR makes
